@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""SAPRC99 cell-solves/s on GB300 (FP64 Rosenbrock, rtol 1e-3, atol 1).
+
+Workload: 262144 synthetic SAPRC99 cells integrated over 24 host steps of
+600 s (seeded draws, see mkpp_gb300/workloads.py).  One bench step is that
+whole integration: restore the initial state, then for each host step compute
+the rate constants from the hour's photolysis and integrate every cell with
+the persistent work-queue kernel.  The 24 host steps are captured once as a
+CUDA graph and each step is one graph launch.  value = cells * host steps /
+step time (cell-solves/s, summed over ranks).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+The JSON line also carries: e2e (the same run through the host-buffer C ABI
+mkpp_integrate, copies included), roofline (FP64 pipe of the integrate kernel
+against a live DFMA probe), cpu_baseline, the plain one-thread-per-cell
+per-launch form for comparison, clocks sampled during the timed region, and
+gpu_launches.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SAPRC99 cell-solves/s on 1 GB300 at rtol 1e-3"
+UNIT = "cell-solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", default="saprc99")
+    ap.add_argument("--cells", type=int, default=None)
+    ap.add_argument("--host-steps", type=int, default=None)
+    ap.add_argument("--cpu-cells", type=int, default=256, help="cells in the bounded CPU sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--max-attempts", type=int, default=100000)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        load = [r for r in rows if r[2] > 200.0] or rows
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in load for n, v in zip(names, r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_sample(w, cells: int, host_steps: int, threads: int):
+    """Time the CPU implementation on the first `cells` cells of the workload."""
+    sub = w.subset(cells)
+    try:
+        from oracle import ref_build
+
+        ref = ref_build.load(sub.mechanism)
+    except Exception:
+        ref = None
+    if ref is not None:
+        kind, runner = "reference", ref
+    else:
+        from oracle.oracle import Oracle
+
+        kind, runner = "port", Oracle(sub.mechanism)
+    conc = sub.conc.copy()
+    t0 = time.perf_counter()
+    for s in range(host_steps):
+        runner.integrate(conc, sub.dt, temp=sub.temp, rho=sub.rho, rh=sub.rh, param=sub.param_at(s),
+                         nthreads=threads)
+        if kind == "port":
+            pass
+    el = time.perf_counter() - t0
+    return kind, cells * host_steps / el, el
+
+
+def run_reference(args, world, rank):
+    from mkpp_gb300 import workloads
+
+    if rank != 0:
+        return
+    w = workloads.make(args.workload, args.cells)
+    hs = args.host_steps or w.host_steps
+    threads = os.cpu_count() or 1
+    vals = []
+    kind = "port"
+    for i in range(args.warmup + args.steps):
+        kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
+        if i >= args.warmup:
+            vals.append((v, el))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(el for _, el in vals) * 1e3
+    sample = f"first {args.cpu_cells} of {w.ncells} cells x {hs} host steps of {w.dt:g} s"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(w, hs),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(w, hs):
+    from mkpp_gb300.emitter.plan import load_raw
+
+    raw = load_raw(w.mechanism)
+    return {"workload": f"{w.mechanism}: {w.ncells} cells x {hs} host steps of {w.dt:g} s, ROS-3, "
+                        f"rtol {raw['rtol'][0]:g}, atol {raw['atol'][0]:g}",
+            "mechanism": w.mechanism, "cells_per_gpu": w.ncells, "host_steps": hs, "dt_s": w.dt,
+            "tableau": raw["tableau"]["name"], "form": "persistent work-queue kernel, 24 host steps in one CUDA graph",
+            "l2": "inputs larger than L2 (concentrations + rate-constant table > 129 MB)"}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    from mkpp_gb300 import workloads
+    from mkpp_gb300.api import MKPP_SUCCESS, DeviceSolver, MechanismContext, load_library
+    from mkpp_gb300.emitter.plan import flops_per_attempt, load, load_raw
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workloads.make(args.workload, args.cells, seed=workloads.SEED + rank)
+    hs = args.host_steps or w.host_steps
+    n = w.ncells
+    raw = load_raw(w.mechanism)
+    plan = load(w.mechanism)
+    lib = load_library(w.mechanism)
+    solver = DeviceSolver(w.mechanism)
+    NS, NR, NP = solver.sizes.species, solver.sizes.reactions, solver.sizes.rate_parameters
+    seed = float(raw["initial_step_seed"])
+
+    f64 = torch.float64
+    conc0 = torch.from_numpy(w.conc).to(dev)
+    conc = conc0.clone()
+    temp = torch.from_numpy(w.temp).to(dev)
+    rho = torch.from_numpy(w.rho).to(dev)
+    rh = torch.from_numpy(w.rh).to(dev)
+    params = torch.from_numpy(np.stack([w.param_at(s) for s in range(hs)])).to(dev)
+    ktab = torch.empty((NR, n), dtype=f64, device=dev)
+    status = torch.zeros(n, dtype=torch.int32, device=dev)
+    acc = torch.zeros((hs, n), dtype=torch.int32, device=dev)
+    rej = torch.zeros((hs, n), dtype=torch.int32, device=dev)
+    ws_bytes = int(lib.mkpp_gpu_workspace_bytes(C.c_size_t(n)))
+    ws = torch.zeros(max(ws_bytes, 256), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def check(rc, what):
+        if rc != MKPP_SUCCESS:
+            raise RuntimeError(f"{what} failed: {rc}")
+
+    def one_run(mode=1, events=None):
+        conc.copy_(conc0)
+        for s in range(hs):
+            check(lib.mkpp_gpu_rate_constants(C.c_size_t(n), p(conc), p(temp), p(rho), p(rh), None, p(params[s]),
+                                              C.c_size_t(NP), p(ktab), p(status), sp), "rate constants")
+            if events is not None:
+                events[s][0].record(stream)
+            check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab), 1, C.c_double(w.dt), C.c_double(seed),
+                                           args.max_attempts, mode, p(status), p(acc[s]), p(rej[s]), p(ws),
+                                           C.c_size_t(ws.numel()), sp), "integrate")
+            if events is not None:
+                events[s][1].record(stream)
+
+    # Warm-up runs, eager, with events around every integrate launch.
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(hs)]
+    kernel_ms = []
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            one_run(1, ev)
+            stream.synchronize()
+            kernel_ms.append([a.elapsed_time(b) for a, b in ev])
+    # Capture the 24 host steps as one graph.
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(g, stream=stream):
+            one_run(1)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks, torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(args.steps):
+            g.replay()
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    el_ms = max_over_ranks(start.elapsed_time(end), world) / args.steps
+    clk = clocks.summary()
+    cell_solves = n * hs * world
+    value = cell_solves / (el_ms * 1e-3)
+
+    # Work counters of the (deterministic) run just timed.
+    acc_h, rej_h = acc.cpu().numpy(), rej.cpu().numpy()
+    st_h = status.cpu().numpy()
+    attempts = int(acc_h.sum()) + int(rej_h.sum())
+    fpa = flops_per_attempt(plan)
+    flops_run = attempts * fpa["total"]
+    # Dominant kernel: the integrate launches; average per launch over the last warm-up run.
+    per_launch_ms = statistics.mean(kernel_ms[-1]) if kernel_ms else float("nan")
+    kernel_total_ms = sum(kernel_ms[-1]) if kernel_ms else float("nan")
+    achieved = flops_run / (kernel_total_ms * 1e-3) / 1e12 if kernel_ms else None
+
+    # Live FP64 FMA peak (DFMA probe on this GPU).
+    probe = C.CDLL(str(ROOT / "mkpp_gb300" / "lib" / "libmkpp_probe.so"))
+    probe.mkpp_probe_fp64_fma.restype = C.c_double
+    probe.mkpp_probe_fp64_fma.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    pout = torch.zeros(sms * 8, dtype=f64, device=dev)
+    best = 0.0
+    with torch.cuda.stream(stream):
+        for _ in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fl = probe.mkpp_probe_fp64_fma(p(pout), sms * 8, 256, 2000, sp)
+            b.record(stream)
+            stream.synchronize()
+            best = max(best, fl / (a.elapsed_time(b) * 1e-3) / 1e12)
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peaks = json.loads(peaks_path.read_text()) if peaks_path.exists() else {}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
+        "gpu_launches": args.steps * hs * 2,
+        "clocks": clk,
+        "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
+                 "failed_cells": int((st_h != 0).sum())},
+        "roofline": {
+            "bound": "fp64", "achieved": achieved, "peak": best, "unit": "TFLOP/s",
+            "frac": (achieved / best) if achieved and best else None,
+            "peak_source": "measured live: DFMA probe (csrc/probe.cu) on this GPU",
+            "kernel": "integrate_persistent_kernel", "launch_ms_avg": per_launch_ms,
+            "algorithmic_flops_per_launch": flops_run / hs,
+            "traffic": None,
+            "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        },
+    }
+
+    if rank == 0 and not args.no_plain:
+        # Plain form: one thread per cell, per-launch, no graph, same inputs.
+        pe = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        with torch.cuda.stream(stream):
+            pe[0].record(stream)
+            one_run(0)
+            pe[1].record(stream)
+            stream.synchronize()
+        pm = pe[0].elapsed_time(pe[1])
+        result["plain_form"] = {"value": n * hs / (pm * 1e-3), "unit": UNIT, "ms_per_step": pm,
+                                "form": "one thread per cell, 48 eager launches"}
+
+    if not args.no_e2e:
+        # End to end through the reference-facing host C ABI with pinned host buffers.
+        host_conc = torch.from_numpy(w.conc).pin_memory()
+        work_conc = host_conc.clone().pin_memory()
+        host_par = [torch.from_numpy(w.param_at(s)).pin_memory() for s in range(hs)]
+        t_h, r_h, p_h = (torch.from_numpy(a).pin_memory() for a in (w.temp, w.rho, w.pressure))
+        rh_h = torch.from_numpy(w.rh).pin_memory()
+        ctx = MechanismContext(w.mechanism, n)
+        conc_np, par_np = work_conc.numpy(), [x.numpy() for x in host_par]
+        ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
+        ctx.set_aerosol(relative_humidity=rh_h.numpy())
+        e2e_times = []
+        for rep in range(2):
+            work_conc.copy_(host_conc)
+            barrier(world)
+            t0 = time.perf_counter()
+            for s in range(hs):
+                ctx.set_rate_parameters(par_np[s])
+                ctx.integrate(w.dt)
+            e2e_times.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(min(e2e_times), world)
+        h2d = hs * n * 8 * (NS + 3 + NP)
+        d2h = hs * n * 8 * NS
+        result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24"}
+        ctx.close()
+
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                                  "sample": f"first {args.cpu_cells} of {n} cells x {hs} host steps of {w.dt:g} s",
+                                  "seconds": el}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

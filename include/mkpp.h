@@ -1,0 +1,149 @@
+/*
+ * mkpp.h - C ABI of one GB300-compiled MKPP mechanism library
+ * (libmkpp_<mechanism>.so).
+ *
+ * The first block is the reference's host API, same symbols, argument meaning
+ * and return codes as the header MKPP emits with `--host-api`
+ * (src/mkpp/templates/host_api/mkpp.h.j2:17-72, implementation
+ * src/mkpp/templates/host_api/mkpp_c_api.cpp.j2:70-374).  Like the reference,
+ * the symbols are not mechanism-namespaced: one mechanism per linked library.
+ * Host buffers stay caller-owned; mkpp_integrate stages them to the GPU,
+ * integrates every cell there and copies the concentrations back before it
+ * returns, so the call keeps the reference's blocking, in-place semantics.
+ *
+ * The second block (mkpp_gpu_*) has no counterpart in the reference: it takes
+ * device pointers, runs on a caller-chosen CUDA stream and never blocks, for
+ * host models that keep their state resident on the GPU.
+ *
+ * Layouts are LayoutLeft with the cell index innermost:
+ *   conc[cell + num_cells * species], param[cell + num_cells * slot],
+ *   jac[cell + num_cells * (row + N * col)].
+ */
+#ifndef MKPP_GB300_MKPP_H
+#define MKPP_GB300_MKPP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return status codes (mkpp.h.j2:17-24). */
+#define MKPP_SUCCESS                  0
+#define MKPP_ERROR_NULL_POINTER     -101
+#define MKPP_ERROR_INVALID_HANDLE   -102
+#define MKPP_ERROR_INVALID_ARGUMENT -103
+#define MKPP_ERROR_INVALID_STATE    -104
+#define MKPP_ERROR_CONVERGENCE      -105
+#define MKPP_ERROR_NOT_FOUND        -106
+/* GPU runtime failure (no reference counterpart). */
+#define MKPP_ERROR_DEVICE           -107
+
+/* Per-cell status codes written by the solver (dispatcher.hpp:15-21). */
+#define MKPP_CELL_SUCCESS               0
+#define MKPP_CELL_ERR_SINGULAR_MATRIX   1
+#define MKPP_CELL_ERR_NON_FINITE_STATE  2
+#define MKPP_CELL_ERR_CONVERGENCE       3
+#define MKPP_CELL_ERR_NUMERICAL         4
+
+typedef struct mkpp_handle_s* mkpp_handle_t;
+
+/* ---- Reference host API (mkpp.h.j2:38-72) ---------------------------- */
+
+/* mkpp.h.j2:38 */
+int mkpp_create_handle(mkpp_handle_t* handle_out, size_t num_cells);
+/* mkpp.h.j2:39 */
+int mkpp_destroy_handle(mkpp_handle_t handle);
+/* mkpp.h.j2:40 */
+int mkpp_initialize(mkpp_handle_t handle);
+/* mkpp.h.j2:43-47 */
+int mkpp_get_species_count(mkpp_handle_t handle, size_t* count_out);
+int mkpp_get_reaction_count(mkpp_handle_t handle, size_t* count_out);
+int mkpp_get_photolysis_count(mkpp_handle_t handle, size_t* count_out);
+int mkpp_get_species_index(mkpp_handle_t handle, const char* species_name, int* index_out);
+int mkpp_get_photolysis_index(mkpp_handle_t handle, const char* photo_name, int* index_out);
+/* mkpp.h.j2:50-54: LayoutLeft (cells x species) concentrations, per-cell T, p, rho. */
+int mkpp_set_state_ptrs(mkpp_handle_t handle, double* species_conc, const double* temp,
+                        const double* pressure, const double* air_density);
+/* mkpp.h.j2:57: values[cell + num_cells * parameter]; count must equal the
+ * mechanism's runtime parameter count. */
+int mkpp_set_rate_parameter_ptrs(mkpp_handle_t handle, const double* values, size_t count);
+/* mkpp.h.j2:59 */
+int mkpp_set_photolysis_ptrs(mkpp_handle_t handle, const double* photolysis_rates);
+/* mkpp.h.j2:61 */
+int mkpp_set_cloud_water_ptr(mkpp_handle_t handle, const double* values);
+/* mkpp.h.j2:63-65 */
+int mkpp_set_aerosol_ptrs(mkpp_handle_t handle, const double* relative_humidity,
+                          const double* aerosol_surface_area);
+/* mkpp.h.j2:68: integrates every cell over dt seconds, in place. */
+int mkpp_integrate(mkpp_handle_t handle, double dt);
+/* mkpp.h.j2:70: species tendencies, (cells x species) LayoutLeft. */
+int mkpp_evaluate_rates(mkpp_handle_t handle, double* rates_out);
+/* mkpp.h.j2:71: dense Jacobian (cells x N x N) LayoutLeft. */
+int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out);
+/* mkpp.h.j2:74 */
+int mkpp_get_last_error(mkpp_handle_t handle, char* buffer, size_t buffer_len);
+
+/* ---- Handle options (no reference C entry; the reference exposes the
+ * seed as the SolverKernels::initial_step_seed member, integrate.j2:42) --- */
+int mkpp_set_initial_step_seed(mkpp_handle_t handle, double seed);
+/* Upper bound on attempts per integrate() call (default 100000). */
+int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts);
+/* Read back the per-cell status / accepted / rejected counts of the last
+ * mkpp_integrate (each array num_cells ints; any may be NULL). */
+int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* rejected);
+
+/* ---- Mechanism metadata (no reference C entry; compile-time constants of
+ * the generated SolverKernels, header.j2:127-186) ------------------------ */
+int mkpp_mechanism_name(const char** name_out);
+/* species, variable species, reactions, runtime parameter slots, LU slots */
+int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions,
+                         int* num_rate_parameters, int* num_lu_slots);
+
+/* ---- Device-pointer entry points (no reference counterpart) ----------- */
+
+/* Workspace bytes mkpp_gpu_integrate_k / _logged need: a queue counter plus
+ * the per-block LU/stage scratch tiles of the integrate grid (sized to this
+ * GPU, independent of num_cells).  The workspace must be 256-byte aligned. */
+size_t mkpp_gpu_workspace_bytes(size_t num_cells);
+
+/* Rate constants of every reaction into ktab[cell + num_cells * reaction].
+ * temp/rho/rh/clw/param may be NULL (compile-time environment, 0.5, 0, zeros).
+ * status (may be NULL) receives MKPP_CELL_ERR_NON_FINITE_STATE for cells with
+ * non-finite inputs, MKPP_CELL_SUCCESS otherwise. */
+int mkpp_gpu_rate_constants(size_t num_cells, const double* conc, const double* temp,
+                            const double* rho, const double* rh, const double* clw,
+                            const double* param, size_t num_params, double* ktab,
+                            int* status, void* stream);
+
+/* Integrate every cell `steps` times over dt seconds from precomputed rate
+ * constants.  mode 0 = one thread per cell (plain), 1 = persistent work queue.
+ * workspace: at least mkpp_gpu_workspace_bytes(num_cells) bytes of device
+ * memory (queue counter and per-block scratch).  Cells whose status is non-zero on entry
+ * are skipped.  Asynchronous on `stream`. */
+int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps,
+                         double dt, double seed, int max_attempts, int mode, int* status,
+                         int* accepted, int* rejected, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* Same as mkpp_gpu_integrate_k, also recording every attempt's step size and
+ * accept flag (log_h/log_acc[attempt * num_cells + cell], log_n[cell]) for
+ * step-sequence replay; plain mode only. */
+int mkpp_gpu_integrate_logged(size_t num_cells, double* conc, const double* ktab, int steps,
+                              double dt, double seed, int max_attempts, int* status,
+                              int* accepted, int* rejected, double* log_h,
+                              unsigned char* log_acc, int* log_n, int log_cap, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
+/* Species tendencies F (LayoutLeft cells x N, fixed species 0) from rate constants. */
+int mkpp_gpu_evaluate_rates(size_t num_cells, const double* conc, const double* ktab,
+                            double* rates_out, void* stream);
+/* Dense Jacobian (cells x N x N LayoutLeft, fixed rows and columns 0). */
+int mkpp_gpu_evaluate_jacobian(size_t num_cells, const double* conc, const double* ktab,
+                               double* jac_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MKPP_GB300_MKPP_H */

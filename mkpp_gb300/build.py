@@ -1,0 +1,112 @@
+"""Build the per-mechanism CUDA libraries (sm_103a) in-tree.
+
+Each mechanism library ``mkpp_gb300/lib/libmkpp_<name>.so`` is one nvcc
+translation unit: ``csrc/mkpp_capi.cu`` with the generated
+``generated/<name>.cuh`` included.  Libraries are rebuilt only when a source
+is newer than the library.  Builds run in parallel.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+GEN = PKG / "generated"
+LIB = PKG / "lib"
+INCLUDE = ROOT / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99")
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build mkpp_gb300")
+
+
+def lib_path(mech: str) -> Path:
+    return LIB / f"libmkpp_{mech}.so"
+
+
+def _sources(mech: str) -> list[Path]:
+    return [CSRC / "mkpp_capi.cu", CSRC / "solver.cuh", CSRC / "mkpp_device.cuh",
+            GEN / f"{mech}.cuh", INCLUDE / "mkpp.h", Path(__file__)]
+
+
+def _stale(mech: str) -> bool:
+    out = lib_path(mech)
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(s.exists() and s.stat().st_mtime > t for s in _sources(mech))
+
+
+def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    out = lib_path(mech)
+    LIB.mkdir(parents=True, exist_ok=True)
+    tmp = out.with_suffix(f".so.tmp{os.getpid()}")
+    cmd = [
+        nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+        "--extended-lambda", "-Xptxas", "-v" if verbose else "-O3",
+        f"-DMKPP_MECH_HEADER=\"{mech}.cuh\"", f"-DMKPP_MECH_NS=mkpp_{mech}",
+        f"-I{GEN}", f"-I{CSRC}", f"-I{INCLUDE}",
+        *(extra or []),
+        str(CSRC / "mkpp_capi.cu"), "-o", str(tmp),
+    ]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        tmp.unlink(missing_ok=True)
+        raise RuntimeError(f"nvcc failed for {mech}:\n{' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
+    if verbose:
+        sys.stderr.write(proc.stderr)
+    os.replace(tmp, out)
+    return out
+
+
+def compile_probe() -> Path:
+    out = LIB / "libmkpp_probe.so"
+    src = CSRC / "probe.cu"
+    if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+        return out
+    LIB.mkdir(parents=True, exist_ok=True)
+    tmp = out.with_suffix(f".so.tmp{os.getpid()}")
+    subprocess.run([nvcc(), *ARCH, "-O3", "-shared", "-Xcompiler", "-fPIC", str(src), "-o", str(tmp)], check=True)
+    os.replace(tmp, out)
+    return out
+
+
+def build(mechanisms=DEFAULT_MECHANISMS, force: bool = False, verbose: bool = False, jobs: int | None = None) -> list[Path]:
+    from .emitter import cuda_emitter
+
+    for m in mechanisms:
+        cuda_emitter.write(m)
+    todo = [m for m in mechanisms if force or _stale(m)]
+    # Largest translation units first so they overlap the small ones.
+    todo.sort(key=lambda m: -(GEN / f"{m}.cuh").stat().st_size)
+    with ThreadPoolExecutor(max_workers=jobs or max(1, min(len(todo) + 1, os.cpu_count() or 4))) as ex:
+        futs = [ex.submit(compile_mechanism, m, verbose) for m in todo]
+        futs.append(ex.submit(compile_probe))
+        for f in futs:
+            f.result()
+    return [lib_path(m) for m in mechanisms]
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("mechanisms", nargs="*", default=list(DEFAULT_MECHANISMS))
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args()
+    for p in build(a.mechanisms, force=a.force, verbose=a.verbose):
+        print(p)

@@ -1,0 +1,645 @@
+// C ABI of one mechanism library (libmkpp_<mechanism>.so), see include/mkpp.h.
+//
+// Compiled once per mechanism with
+//   -DMKPP_MECH_HEADER="<mechanism>.cuh" -DMKPP_MECH_NS=mkpp_<mechanism>
+// The host-buffer entry points follow the reference implementation
+// (src/mkpp/templates/host_api/mkpp_c_api.cpp.j2:70-374): same argument
+// checks, the same "FATAL ERROR:" messages in mkpp_get_last_error and the same
+// return codes.  mkpp_integrate stages the caller's host arrays to device
+// memory owned by the handle, runs the GPU solve on the handle's stream and
+// copies the concentrations back before returning.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/mkpp.h"
+#include "solver.cuh"
+#include MKPP_MECH_HEADER
+
+using Mech = MKPP_MECH_NS::Mech;
+
+namespace {
+
+constexpr int kDefaultMaxAttempts = 100000;
+
+struct DeviceBuffers {
+  size_t cells = 0;
+  double* conc = nullptr;
+  double* temp = nullptr;
+  double* rho = nullptr;
+  double* rh = nullptr;
+  double* clw = nullptr;
+  double* param = nullptr;
+  double* ktab = nullptr;
+  double* out = nullptr;      // rates / Jacobian staging
+  size_t out_bytes = 0;
+  int* status = nullptr;
+  int* accepted = nullptr;
+  int* rejected = nullptr;
+  void* workspace = nullptr;
+};
+
+}  // namespace
+
+struct mkpp_handle_s {
+  size_t num_cells = 0;
+  bool initialized = false;
+  double* conc = nullptr;
+  const double* temp = nullptr;
+  const double* pressure = nullptr;
+  const double* rho = nullptr;
+  const double* rh = nullptr;
+  const double* sa = nullptr;
+  const double* clw = nullptr;
+  const double* param = nullptr;
+  size_t param_count = 0;
+  double seed = Mech::SEED;
+  int max_attempts = kDefaultMaxAttempts;
+  int mode = 1;  // persistent queue
+  cudaStream_t stream = nullptr;
+  DeviceBuffers dev;
+  std::string last_error;
+
+  void set_error(const std::string& msg) { last_error = msg; }
+};
+
+namespace {
+
+int device_fail(mkpp_handle_s* h, cudaError_t err, const char* what) {
+  if (h) h->set_error(std::string("FATAL ERROR: ") + what + ": " + cudaGetErrorString(err));
+  return MKPP_ERROR_DEVICE;
+}
+
+#define MKPP_CUDA(h, call)                                      \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return device_fail((h), e_, #call);  \
+  } while (0)
+
+int launch_grid(size_t cells, int block) { return (int)std::max<size_t>(1, (cells + block - 1) / block); }
+
+using StoreInfo = mkpp::StoreFor<Mech>;
+constexpr size_t kQueueBytes = 256;
+
+// Grid of the plain and persistent integrate kernels: SMs x resident blocks
+// per SM.  MKPP_BLOCKS_PER_SM caps the residency (fewer blocks keep the
+// per-block scratch tiles of large mechanisms closer to L2).
+int integrate_grid() {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0, per_sm_plain = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mkpp::integrate_persistent_kernel<Mech>, mkpp::kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_plain, mkpp::integrate_plain_kernel<Mech>, mkpp::kBlock, 0);
+    per_sm = std::max(1, std::min(per_sm, per_sm_plain));
+    if (const char* env = std::getenv("MKPP_BLOCKS_PER_SM")) {
+      const int cap = std::atoi(env);
+      if (cap > 0) per_sm = std::min(per_sm, cap);
+    }
+    grid = std::max(1, sms) * per_sm;
+  }
+  return grid;
+}
+
+size_t workspace_bytes() { return kQueueBytes + (size_t)integrate_grid() * StoreInfo::block_bytes; }
+
+int launch_rates(size_t cells, const double* conc, const double* temp, const double* rho,
+                 const double* rh, const double* clw, const double* param, double* ktab,
+                 int* status, cudaStream_t stream) {
+  mkpp::RateArgs a;
+  a.ncells = (int)cells;
+  a.conc = conc;
+  a.param = param;
+  a.temp = Mech::RUNTIME_ENV ? temp : nullptr;
+  a.rho = Mech::RUNTIME_ENV ? rho : nullptr;
+  a.rh = rh;
+  a.clw = clw;
+  a.ktab = ktab;
+  a.status = status;
+  mkpp::rate_constant_kernel<Mech><<<launch_grid(cells, 128), 128, 0, stream>>>(a);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+// workspace: [queue counter | per-block scratch tiles], workspace_bytes() long.
+int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cudaStream_t stream) {
+  mkpp::LaunchArgs a = args;
+  unsigned char* ws = (unsigned char*)workspace;
+  a.queue = (unsigned int*)ws;
+  double* scratch = StoreInfo::block_bytes ? (double*)(ws + kQueueBytes) : nullptr;
+  if (mode == 1) {
+    if (cudaMemsetAsync(a.queue, 0, sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
+    mkpp::integrate_persistent_kernel<Mech><<<integrate_grid(), mkpp::kBlock, 0, stream>>>(a, scratch);
+  } else {
+    mkpp::integrate_plain_kernel<Mech><<<integrate_grid(), mkpp::kBlock, 0, stream>>>(a, scratch);
+  }
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+mkpp::LaunchArgs make_args(size_t cells, double* conc, const double* ktab, int steps, double dt, double seed,
+                           int max_attempts, int* status, int* accepted, int* rejected) {
+  mkpp::LaunchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.ncells = (int)cells;
+  a.steps = steps;
+  a.dt = dt;
+  a.seed = seed;
+  a.max_attempts = max_attempts;
+  a.conc = conc;
+  a.ktab = ktab;
+  a.status = status;
+  a.n_accept = accepted;
+  a.n_reject = rejected;
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// Tendency and dense-Jacobian evaluation (compute_rates / compute_jacobian,
+// src/mkpp/templates/kernel_functions/compute_{rates,jacobian}.j2).
+// ---------------------------------------------------------------------------
+// State accessor over a cell's row of the (species x cells) array.
+struct CellState {
+  const double* conc;
+  size_t c, n;
+  __device__ __forceinline__ double operator()(int i) const { return conc[c + n * Mech::var_phys(i)]; }
+};
+
+__global__ void __launch_bounds__(128, 1) eval_rates_kernel(size_t n, const double* conc, const double* ktab,
+                                                         double* out) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const mkpp::KTable k{ktab + c, n};
+  for (int s = 0; s < Mech::NS; ++s) out[c + n * s] = 0.0;
+  Mech::fun(CellState{conc, c, n}, k, [&](int i, double v) { out[c + n * Mech::var_phys(i)] = v; });
+}
+
+// Writes W slots straight into the dense (cells x N x N) LayoutLeft output.
+struct DenseSlots {
+  double* out;
+  size_t c, n;
+  __device__ __forceinline__ double& operator[](int s) const {
+    return out[c + n * ((size_t)Mech::lu_prow(s) + (size_t)Mech::NS * Mech::lu_pcol(s))];
+  }
+};
+
+__global__ void __launch_bounds__(128, 1) eval_jacobian_kernel(size_t n, const double* conc, const double* ktab,
+                                                            double* out) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const mkpp::KTable k{ktab + c, n};
+  const size_t NS = Mech::NS;
+  for (size_t e = 0; e < NS * NS; ++e) out[c + n * e] = 0.0;
+  DenseSlots S{out, c, n};
+  // W with inv_g_dt = 0 is -J on the W slots; flip the sign afterwards.
+  Mech::jac_w(CellState{conc, c, n}, k, 0.0, S);
+  Mech::for_each_w_slot([&](int slot, int, int) { S[slot] = -S[slot]; });
+}
+
+__global__ void __launch_bounds__(128, 1) mkpp_fixed_columns_kernel(size_t n, const double* conc, const double* temp,
+                                                                 const double* rho, const double* rh,
+                                                                 const double* clw, const double* param,
+                                                                 double* out) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const CellState y{conc, c, n};
+  const double T = (Mech::RUNTIME_ENV && temp) ? temp[c] : Mech::ENV_T;
+  const double RHO = (Mech::RUNTIME_ENV && rho) ? rho[c] : Mech::ENV_RHO;
+  const double RH = rh ? rh[c] : 0.5;
+  const double CLW = clw ? clw[c] : 0.0;
+  const mkpp::CellRow fix{conc + c, n};
+  const size_t NS = Mech::NS;
+  auto put = [&](int row, int col, double v) { out[c + n * (row + NS * col)] = v; };
+  if (param) {
+    const mkpp::CellRow P{param + c, n};
+    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
+  } else {
+    const mkpp::ZeroRow P;
+    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- Reference host API ---------------------------------------------------
+
+int mkpp_create_handle(mkpp_handle_t* handle_out, size_t num_cells) {
+  if (!handle_out) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (num_cells > (size_t)INT32_MAX) return MKPP_ERROR_INVALID_ARGUMENT;
+  auto* h = new (std::nothrow) mkpp_handle_s();
+  if (!h) return MKPP_ERROR_INVALID_STATE;
+  h->num_cells = num_cells;
+  *handle_out = h;
+  return MKPP_SUCCESS;
+}
+
+static void free_device(DeviceBuffers& d) {
+  cudaFree(d.conc);
+  cudaFree(d.temp);
+  cudaFree(d.rho);
+  cudaFree(d.rh);
+  cudaFree(d.clw);
+  cudaFree(d.param);
+  cudaFree(d.ktab);
+  cudaFree(d.out);
+  cudaFree(d.status);
+  cudaFree(d.accepted);
+  cudaFree(d.rejected);
+  cudaFree(d.workspace);
+  d = DeviceBuffers();
+}
+
+int mkpp_destroy_handle(mkpp_handle_t handle) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  free_device(handle->dev);
+  if (handle->stream) cudaStreamDestroy(handle->stream);
+  delete handle;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_initialize(mkpp_handle_t handle) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  if (!handle->stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&handle->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return device_fail(handle, e, "cudaStreamCreateWithFlags");
+  }
+  handle->initialized = true;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_species_count(mkpp_handle_t handle, size_t* count_out) {
+  if (!handle || !count_out) return MKPP_ERROR_NULL_POINTER;
+  *count_out = Mech::NS;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_reaction_count(mkpp_handle_t handle, size_t* count_out) {
+  if (!handle || !count_out) return MKPP_ERROR_NULL_POINTER;
+  *count_out = Mech::NR;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_photolysis_count(mkpp_handle_t handle, size_t* count_out) {
+  if (!handle || !count_out) return MKPP_ERROR_NULL_POINTER;
+  *count_out = Mech::NPH;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_species_index(mkpp_handle_t handle, const char* name, int* index_out) {
+  if (!handle || !name || !index_out) return MKPP_ERROR_NULL_POINTER;
+  for (int s = 0; s < Mech::NS; ++s) {
+    if (std::strcmp(Mech::species_name(s), name) == 0) {
+      *index_out = s;
+      return MKPP_SUCCESS;
+    }
+  }
+  *index_out = -1;
+  return MKPP_ERROR_NOT_FOUND;
+}
+
+int mkpp_get_photolysis_index(mkpp_handle_t handle, const char* name, int* index_out) {
+  if (!handle || !name || !index_out) return MKPP_ERROR_NULL_POINTER;
+  for (int p = 0; p < Mech::NPH; ++p) {
+    if (std::strcmp(Mech::photolysis_name(p), name) == 0) {
+      *index_out = p;
+      return MKPP_SUCCESS;
+    }
+  }
+  *index_out = -1;
+  return MKPP_ERROR_NOT_FOUND;
+}
+
+static int validate_state(mkpp_handle_s& h) {
+  if (!h.conc) {
+    h.set_error("FATAL ERROR: species concentration pointer is not bound");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  if (!h.temp || !h.rho || !h.pressure) {
+    h.set_error("FATAL ERROR: per-cell meteorology is not bound");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  for (size_t c = 0; c < h.num_cells; ++c) {
+    if (!std::isfinite(h.temp[c]) || h.temp[c] <= 0.0 || !std::isfinite(h.rho[c]) || h.rho[c] <= 0.0 ||
+        !std::isfinite(h.pressure[c]) || h.pressure[c] <= 0.0) {
+      h.set_error("FATAL ERROR: cell temperature, density and pressure must be positive and finite");
+      return MKPP_ERROR_INVALID_ARGUMENT;
+    }
+  }
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_state_ptrs(mkpp_handle_t handle, double* species_conc, const double* temp,
+                        const double* pressure, const double* air_density) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  if (!species_conc || !temp || !pressure || !air_density) {
+    handle->set_error("FATAL ERROR: state binding requires concentration and meteorology pointers");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  handle->conc = species_conc;
+  handle->temp = temp;
+  handle->pressure = pressure;
+  handle->rho = air_density;
+  return validate_state(*handle);
+}
+
+int mkpp_set_rate_parameter_ptrs(mkpp_handle_t handle, const double* values, size_t count) {
+  if (!handle || !values) return MKPP_ERROR_NULL_POINTER;
+  if (count != (size_t)Mech::NP) {
+    handle->set_error("FATAL ERROR: runtime parameter count does not match the generated mechanism");
+    return MKPP_ERROR_INVALID_ARGUMENT;
+  }
+  handle->param = values;
+  handle->param_count = count;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_photolysis_ptrs(mkpp_handle_t handle, const double* photolysis_rates) {
+  if (!handle || !photolysis_rates) return MKPP_ERROR_NULL_POINTER;
+  if (Mech::NP > Mech::NPH) {
+    handle->set_error("FATAL ERROR: use mkpp_set_rate_parameter_ptrs for the complete runtime parameter array");
+    return MKPP_ERROR_INVALID_ARGUMENT;
+  }
+  return mkpp_set_rate_parameter_ptrs(handle, photolysis_rates, Mech::NPH);
+}
+
+int mkpp_set_cloud_water_ptr(mkpp_handle_t handle, const double* values) {
+  if (!handle || !values) return MKPP_ERROR_NULL_POINTER;
+  handle->clw = values;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_aerosol_ptrs(mkpp_handle_t handle, const double* relative_humidity,
+                          const double* aerosol_surface_area) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  if (relative_humidity) handle->rh = relative_humidity;
+  if (aerosol_surface_area) handle->sa = aerosol_surface_area;
+  return MKPP_SUCCESS;
+}
+
+static int ensure_device(mkpp_handle_s* h, size_t out_bytes) {
+  DeviceBuffers& d = h->dev;
+  const size_t n = h->num_cells;
+  if (d.cells != n) {
+    free_device(d);
+    MKPP_CUDA(h, cudaMalloc(&d.conc, n * Mech::NS * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.temp, n * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.rho, n * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.rh, n * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.clw, n * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.param, n * std::max(1, Mech::NP) * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.ktab, n * Mech::NR * sizeof(double)));
+    MKPP_CUDA(h, cudaMalloc(&d.status, n * sizeof(int)));
+    MKPP_CUDA(h, cudaMalloc(&d.accepted, n * sizeof(int)));
+    MKPP_CUDA(h, cudaMalloc(&d.rejected, n * sizeof(int)));
+    MKPP_CUDA(h, cudaMalloc(&d.workspace, workspace_bytes()));
+    d.cells = n;
+  }
+  if (out_bytes > d.out_bytes) {
+    cudaFree(d.out);
+    d.out = nullptr;
+    d.out_bytes = 0;
+    MKPP_CUDA(h, cudaMalloc(&d.out, out_bytes));
+    d.out_bytes = out_bytes;
+  }
+  return MKPP_SUCCESS;
+}
+
+// Copy the bound host inputs to the device and compute the rate constants.
+static int stage_inputs(mkpp_handle_s* h) {
+  DeviceBuffers& d = h->dev;
+  const size_t n = h->num_cells;
+  cudaStream_t s = h->stream;
+  MKPP_CUDA(h, cudaMemcpyAsync(d.conc, h->conc, n * Mech::NS * sizeof(double), cudaMemcpyHostToDevice, s));
+  MKPP_CUDA(h, cudaMemcpyAsync(d.temp, h->temp, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  MKPP_CUDA(h, cudaMemcpyAsync(d.rho, h->rho, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (h->rh) MKPP_CUDA(h, cudaMemcpyAsync(d.rh, h->rh, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (h->clw) MKPP_CUDA(h, cudaMemcpyAsync(d.clw, h->clw, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (h->param && Mech::NP > 0)
+    MKPP_CUDA(h, cudaMemcpyAsync(d.param, h->param, n * Mech::NP * sizeof(double), cudaMemcpyHostToDevice, s));
+  int rc = launch_rates(n, d.conc, d.temp, d.rho, h->rh ? d.rh : nullptr, h->clw ? d.clw : nullptr,
+                        h->param ? d.param : nullptr, d.ktab, d.status, s);
+  if (rc != MKPP_SUCCESS) return device_fail(h, cudaGetLastError(), "rate_constant_kernel launch");
+  return MKPP_SUCCESS;
+}
+
+int mkpp_integrate(mkpp_handle_t handle, double dt) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  mkpp_handle_s* h = handle;
+  if (!h->initialized) {
+    h->set_error("FATAL ERROR: MKPP handle must be initialized before integration");
+    return MKPP_ERROR_INVALID_STATE;
+  }
+  const int vs = validate_state(*h);
+  if (vs != MKPP_SUCCESS) return vs;
+  if (!std::isfinite(dt) || dt <= 0.0) return MKPP_ERROR_INVALID_ARGUMENT;
+  int rc = ensure_device(h, 0);
+  if (rc != MKPP_SUCCESS) return rc;
+  rc = stage_inputs(h);
+  if (rc != MKPP_SUCCESS) return rc;
+  DeviceBuffers& d = h->dev;
+  const size_t n = h->num_cells;
+  rc = launch_integrate(make_args(n, d.conc, d.ktab, 1, dt, h->seed, h->max_attempts, d.status, d.accepted,
+                                  d.rejected),
+                        h->mode, d.workspace, h->stream);
+  if (rc != MKPP_SUCCESS) return device_fail(h, cudaGetLastError(), "integrate kernel launch");
+  MKPP_CUDA(h, cudaMemcpyAsync(h->conc, d.conc, n * Mech::NS * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MKPP_SUCCESS;
+}
+
+int mkpp_evaluate_rates(mkpp_handle_t handle, double* rates_out) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  mkpp_handle_s* h = handle;
+  if (!rates_out) {
+    h->set_error("FATAL ERROR: rates output pointer is null");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  if (!h->initialized) {
+    h->set_error("FATAL ERROR: MKPP handle must be initialized before rates evaluation");
+    return MKPP_ERROR_INVALID_STATE;
+  }
+  const int vs = validate_state(*h);
+  if (vs != MKPP_SUCCESS) return vs;
+  const size_t n = h->num_cells;
+  const size_t bytes = n * Mech::NS * sizeof(double);
+  int rc = ensure_device(h, bytes);
+  if (rc != MKPP_SUCCESS) return rc;
+  rc = stage_inputs(h);
+  if (rc != MKPP_SUCCESS) return rc;
+  eval_rates_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(n, h->dev.conc, h->dev.ktab, h->dev.out);
+  MKPP_CUDA(h, cudaGetLastError());
+  MKPP_CUDA(h, cudaMemcpyAsync(rates_out, h->dev.out, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MKPP_SUCCESS;
+}
+
+int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  mkpp_handle_s* h = handle;
+  if (!jac_out) {
+    h->set_error("FATAL ERROR: Jacobian output pointer is null");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  if (!h->initialized) {
+    h->set_error("FATAL ERROR: MKPP handle must be initialized before Jacobian evaluation");
+    return MKPP_ERROR_INVALID_STATE;
+  }
+  const int vs = validate_state(*h);
+  if (vs != MKPP_SUCCESS) return vs;
+  const size_t n = h->num_cells;
+  const size_t bytes = n * Mech::NS * Mech::NS * sizeof(double);
+  int rc = ensure_device(h, bytes);
+  if (rc != MKPP_SUCCESS) return rc;
+  rc = stage_inputs(h);
+  if (rc != MKPP_SUCCESS) return rc;
+  eval_jacobian_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(n, h->dev.conc, h->dev.ktab, h->dev.out);
+  MKPP_CUDA(h, cudaGetLastError());
+  if (Mech::NFIX > 0) {
+    mkpp_fixed_columns_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(
+        n, h->dev.conc, h->dev.temp, h->dev.rho, h->rh ? h->dev.rh : nullptr, h->clw ? h->dev.clw : nullptr,
+        h->param ? h->dev.param : nullptr, h->dev.out);
+    MKPP_CUDA(h, cudaGetLastError());
+  }
+  MKPP_CUDA(h, cudaMemcpyAsync(jac_out, h->dev.out, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_last_error(mkpp_handle_t handle, char* buffer, size_t buffer_len) {
+  if (!handle || !buffer || buffer_len == 0) return MKPP_ERROR_NULL_POINTER;
+  std::strncpy(buffer, handle->last_error.c_str(), buffer_len - 1);
+  buffer[buffer_len - 1] = '\0';
+  return MKPP_SUCCESS;
+}
+
+// ---- Handle options -------------------------------------------------------
+
+int mkpp_set_initial_step_seed(mkpp_handle_t handle, double seed) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  if (!std::isfinite(seed) || seed <= 0.0) {
+    handle->set_error("FATAL ERROR: initial_step_seed must be a finite positive fraction of the chemistry interval");
+    return MKPP_ERROR_INVALID_ARGUMENT;
+  }
+  handle->seed = seed;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  if (max_attempts <= 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  handle->max_attempts = max_attempts;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* rejected) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  mkpp_handle_s* h = handle;
+  if (h->dev.cells == 0) {
+    h->set_error("FATAL ERROR: no integration has run on this handle");
+    return MKPP_ERROR_INVALID_STATE;
+  }
+  const size_t bytes = h->num_cells * sizeof(int);
+  if (status) MKPP_CUDA(h, cudaMemcpyAsync(status, h->dev.status, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (accepted) MKPP_CUDA(h, cudaMemcpyAsync(accepted, h->dev.accepted, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (rejected) MKPP_CUDA(h, cudaMemcpyAsync(rejected, h->dev.rejected, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MKPP_SUCCESS;
+}
+
+// ---- Mechanism metadata ----------------------------------------------------
+
+int mkpp_mechanism_name(const char** name_out) {
+  if (!name_out) return MKPP_ERROR_NULL_POINTER;
+  *name_out = Mech::NAME;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions, int* num_rate_parameters,
+                         int* num_lu_slots) {
+  if (num_species) *num_species = Mech::NS;
+  if (num_variable) *num_variable = Mech::NV;
+  if (num_reactions) *num_reactions = Mech::NR;
+  if (num_rate_parameters) *num_rate_parameters = Mech::NP;
+  if (num_lu_slots) *num_lu_slots = Mech::NLU;
+  return MKPP_SUCCESS;
+}
+
+// ---- Device-pointer entry points --------------------------------------------
+
+size_t mkpp_gpu_workspace_bytes(size_t num_cells) {
+  (void)num_cells;  // the integrate grid is sized to the GPU, not to the cells
+  return workspace_bytes();
+}
+
+int mkpp_gpu_rate_constants(size_t num_cells, const double* conc, const double* temp, const double* rho,
+                            const double* rh, const double* clw, const double* param, size_t num_params,
+                            double* ktab, int* status, void* stream) {
+  if (!conc || !ktab) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0 || num_cells > (size_t)INT32_MAX) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (param && num_params != (size_t)Mech::NP) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (Mech::RUNTIME_ENV && (!temp || !rho)) return MKPP_ERROR_NULL_POINTER;
+  return launch_rates(num_cells, conc, temp, rho, rh, clw, param, ktab, status, (cudaStream_t)stream);
+}
+
+static int check_integrate_args(size_t num_cells, const double* conc, const double* ktab, int steps, double dt,
+                                double seed, int max_attempts, const void* workspace, size_t workspace_bytes_) {
+  if (!conc || !ktab || !workspace) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0 || num_cells > (size_t)INT32_MAX) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (!std::isfinite(dt) || dt <= 0.0 || steps < 1 || !(seed > 0.0) || max_attempts < 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (workspace_bytes_ < workspace_bytes()) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (((uintptr_t)workspace) % 256 != 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps, double dt, double seed,
+                         int max_attempts, int mode, int* status, int* accepted, int* rejected, void* workspace,
+                         size_t workspace_bytes_, void* stream) {
+  const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
+  if (rc != MKPP_SUCCESS) return rc;
+  if (mode != 0 && mode != 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  return launch_integrate(make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected),
+                          mode, workspace, (cudaStream_t)stream);
+}
+
+int mkpp_gpu_integrate_logged(size_t num_cells, double* conc, const double* ktab, int steps, double dt, double seed,
+                              int max_attempts, int* status, int* accepted, int* rejected, double* log_h,
+                              unsigned char* log_acc, int* log_n, int log_cap, void* workspace,
+                              size_t workspace_bytes_, void* stream) {
+  const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
+  if (rc != MKPP_SUCCESS) return rc;
+  if (!log_h || !log_acc || !log_n) return MKPP_ERROR_NULL_POINTER;
+  if (log_cap < 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
+  a.log_h = log_h;
+  a.log_acc = log_acc;
+  a.log_n = log_n;
+  a.log_cap = log_cap;
+  return launch_integrate(a, 0, workspace, (cudaStream_t)stream);
+}
+
+int mkpp_gpu_evaluate_rates(size_t num_cells, const double* conc, const double* ktab, double* rates_out,
+                            void* stream) {
+  if (!conc || !ktab || !rates_out) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  eval_rates_kernel<<<launch_grid(num_cells, 128), 128, 0, (cudaStream_t)stream>>>(num_cells, conc, ktab, rates_out);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+int mkpp_gpu_evaluate_jacobian(size_t num_cells, const double* conc, const double* ktab, double* jac_out,
+                               void* stream) {
+  if (!conc || !ktab || !jac_out) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  eval_jacobian_kernel<<<launch_grid(num_cells, 128), 128, 0, (cudaStream_t)stream>>>(num_cells, conc, ktab,
+                                                                                      jac_out);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+}  // extern "C"

@@ -1,0 +1,341 @@
+// Mechanism-independent Rosenbrock driver kernels (sm_103a, FP64).
+//
+// Data layout in HBM (all LayoutLeft, cell index innermost, so a warp's 32
+// lanes touch 32 consecutive doubles of the same species / reaction row):
+//   conc   [NS][ncells]   species concentrations, updated in place
+//   param  [NP][ncells]   runtime parameters (photolysis J, external rates)
+//   ktab   [NR][ncells]   rate constants, written by rate_constant_kernel
+//   temp/rho/rh/clw [ncells]
+//
+// One thread owns one cell.  The per-cell controller reproduces
+// SolverKernels::integrate (src/mkpp/templates/solver_variants/integrate.j2:71-84,
+// 324-379): dt0 = dt_total * seed, h_min = dt_total * 1e-15,
+// dt = min(dt, dt_total - t), factor clamp [0.2, 6], no growth right after a
+// rejection, tenfold cut after two consecutive rejections.  Unlike the
+// reference, every integrate() call is bounded by max_attempts; a cell that
+// hits the bound stops with CELL_ERR_CONVERGENCE_FAILURE instead of spinning.
+#pragma once
+#include <type_traits>
+
+#include "mkpp_device.cuh"
+
+namespace mkpp {
+
+struct LaunchArgs {
+  int ncells;
+  int steps;                 // integrate() calls per cell with the same forcing
+  double dt;                 // dt_total of each call [s]
+  double seed;               // initial_step_seed
+  int max_attempts;          // per integrate() call
+  double* conc;              // [NS][ncells]
+  const double* ktab;        // [NR][ncells]
+  int* status;               // [ncells] or null
+  int* n_accept;             // [ncells] or null (accumulated over steps)
+  int* n_reject;             // [ncells] or null
+  unsigned int* queue;       // persistent kernel work counter (zeroed before launch)
+  // Optional per-attempt log for step-sequence replay in the CPU oracle:
+  // entry a of cell c at [a * ncells + c]; log_n[c] = attempts recorded.
+  double* log_h;
+  unsigned char* log_acc;
+  int* log_n;
+  int log_cap;
+};
+
+struct RateArgs {
+  int ncells;
+  const double* conc;        // [NS][ncells]  (fixed species are read here)
+  const double* param;       // [NP][ncells] or null (zeros)
+  const double* temp;        // [ncells] or null (compile-time environment)
+  const double* rho;         // [ncells] or null
+  const double* rh;          // [ncells] or null (0.5)
+  const double* clw;         // [ncells] or null (0.0)
+  double* ktab;              // [NR][ncells]
+  int* status;               // [ncells] or null: non-finite inputs are flagged
+};
+
+// ---------------------------------------------------------------------------
+// Rate constants: one thread per cell, k_r for every reaction.
+// ---------------------------------------------------------------------------
+struct ZeroRow {
+  __device__ __forceinline__ double operator()(int) const { return 0.0; }
+};
+
+template <class Mech>
+__global__ void __launch_bounds__(128, 1) rate_constant_kernel(RateArgs a) {
+  const size_t n = (size_t)a.ncells;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double T = a.temp ? a.temp[c] : Mech::ENV_T;
+    const double RHO = a.rho ? a.rho[c] : Mech::ENV_RHO;
+    const double RH = a.rh ? a.rh[c] : 0.5;
+    const double CLW = a.clw ? a.clw[c] : 0.0;
+    CellRow fix{a.conc + c, n};
+    CellRowOut k{a.ktab + c, n};
+    if (a.param) {
+      CellRow P{a.param + c, n};
+      Mech::rate_constants(P, fix, T, RHO, RH, CLW, k);
+    } else {
+      ZeroRow P;
+      Mech::rate_constants(P, fix, T, RHO, RH, CLW, k);
+    }
+    if (a.status) {
+      bool ok = finite(T) && finite(RHO);
+#pragma unroll 1
+      for (int s = 0; s < Mech::NS; ++s) ok = ok && finite(a.conc[c + n * s]);
+#pragma unroll 1
+      for (int r = 0; r < Mech::NR; ++r) ok = ok && finite(a.ktab[c + n * r]);
+      a.status[c] = ok ? CELL_SUCCESS : CELL_ERR_NON_FINITE_STATE;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-cell working storage (LU factors, state, stage vectors).
+//
+// Small mechanisms keep it in a private array that the compiler promotes to
+// registers.  Large ones use a slice of a global-memory tile owned by the
+// thread's block, laid out [slot][thread] so that a warp's access to one slot
+// is 32 consecutive doubles and every slot address is an immediate offset
+// from the thread's base pointer.
+// ---------------------------------------------------------------------------
+constexpr int kBlock = 128;
+constexpr int kRegisterSlots = 96;
+
+template <int N>
+struct RegStore {
+  double v[N];
+  __device__ __forceinline__ double& operator[](int s) { return v[s]; }
+};
+
+struct TileStore {
+  double* __restrict__ p;
+  __device__ __forceinline__ double& operator[](int s) const { return p[(size_t)s * kBlock]; }
+};
+
+template <class Mech>
+struct StoreFor {
+  static constexpr bool kTile = Mech::NSLOTS > kRegisterSlots;
+  using type = typename std::conditional<kTile, TileStore, RegStore<(kTile ? 1 : Mech::NSLOTS)>>::type;
+  // Global scratch bytes per block (zero when the store lives in registers).
+  static constexpr size_t block_bytes = kTile ? (size_t)Mech::NSLOTS * kBlock * sizeof(double) : 0;
+};
+
+template <class Mech>
+__device__ __forceinline__ TileStore make_store(double* scratch, TileStore*) {
+  return TileStore{scratch + (size_t)blockIdx.x * Mech::NSLOTS * kBlock + threadIdx.x};
+}
+template <class Mech, int N>
+__device__ __forceinline__ RegStore<N> make_store(double*, RegStore<N>*) {
+  return RegStore<N>{};
+}
+
+// ---------------------------------------------------------------------------
+// Per-cell controller state and one controller step.
+// ---------------------------------------------------------------------------
+struct Controller {
+  double t, dt, dt_total, h_min;
+  bool reject_last, reject_more;
+  int attempts;
+
+  __device__ __forceinline__ void start(double total, double seed) {
+    dt_total = total;
+    h_min = total * 1.0e-15;
+    t = 0.0;
+    dt = total * seed;
+    reject_last = reject_more = false;
+    attempts = 0;
+  }
+  __device__ __forceinline__ bool running() const { return t < dt_total; }
+  // Step size of the next attempt (integrate.j2:85: dt = min(dt, dt_total - t)).
+  __device__ __forceinline__ double next_h() {
+    dt = fmin(dt, dt_total - t);
+    return dt;
+  }
+  // Accept/reject bookkeeping (integrate.j2:335-379); returns true on accept.
+  template <class Mech>
+  __device__ __forceinline__ bool update(double err) {
+    const double factor = Mech::growth(err);
+    ++attempts;
+    if (err <= 1.0) {
+      t += dt;
+      double next_dt = fmax(h_min, fmin(dt * factor, dt_total));
+      if (reject_last) next_dt = fmin(next_dt, dt);
+      reject_last = false;
+      reject_more = false;
+      dt = next_dt;
+      return true;
+    }
+    dt *= reject_more ? 0.1 : factor;
+    reject_more = reject_last;
+    reject_last = true;
+    return false;
+  }
+};
+
+template <class Mech, class SA>
+__device__ __forceinline__ void load_state(const double* conc, size_t c, size_t n, SA& S) {
+#pragma unroll
+  for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] = conc[c + n * Mech::var_phys(i)];
+}
+
+template <class Mech, class SA>
+__device__ __forceinline__ void store_state(double* conc, size_t c, size_t n, SA& S) {
+#pragma unroll
+  for (int i = 0; i < Mech::NV; ++i) conc[c + n * Mech::var_phys(i)] = S[Mech::Y + i];
+}
+
+template <class Mech, class SA>
+__device__ __forceinline__ bool state_finite(SA& S) {
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < Mech::NV; ++i) ok = ok && finite(S[Mech::Y + i]);
+  return ok;
+}
+
+template <class Mech, class SA>
+__device__ __forceinline__ void apply_increment(SA& S) {
+#pragma unroll
+  for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] += S[Mech::DY + i];
+}
+
+// One cell, `steps` integrate() calls; the plain kernel's per-cell body.
+template <class Mech, class SA, class KA>
+__device__ __forceinline__ int integrate_cell(SA& S, const KA& k, const LaunchArgs& a, size_t c, int& nacc,
+                                              int& nrej) {
+  const size_t n = (size_t)a.ncells;
+  int status = CELL_SUCCESS, logged = 0;
+  nacc = nrej = 0;
+  for (int step = 0; step < a.steps && status == CELL_SUCCESS; ++step) {
+    Controller ctl;
+    ctl.start(a.dt, a.seed);
+    while (ctl.running()) {
+      if (ctl.attempts >= a.max_attempts) {
+        status = CELL_ERR_CONVERGENCE_FAILURE;
+        break;
+      }
+      const double h = ctl.next_h();
+      int st = 0;
+      const double err = Mech::attempt(S, k, h, st);
+      if (st) status = CELL_ERR_SINGULAR_MATRIX;
+      const bool acc = ctl.update<Mech>(err);
+      if (a.log_h && logged < a.log_cap) {
+        a.log_h[(size_t)logged * n + c] = h;
+        a.log_acc[(size_t)logged * n + c] = acc ? 1 : 0;
+        ++logged;
+      }
+      if (acc) {
+        apply_increment<Mech>(S);
+        ++nacc;
+      } else {
+        ++nrej;
+      }
+    }
+  }
+  if (a.log_n) a.log_n[c] = logged;
+  if (status == CELL_SUCCESS && !state_finite<Mech>(S)) status = CELL_ERR_NUMERICAL_FAILURE;
+  return status;
+}
+
+// ---------------------------------------------------------------------------
+// Plain form: a fixed grid, thread t integrates cells t, t + T, t + 2T, ...
+// (T = grid threads) one after the other.  A warp runs until its slowest
+// lane is done, so lanes with easy cells idle while stiff ones finish.
+// ---------------------------------------------------------------------------
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 1) integrate_plain_kernel(LaunchArgs a, double* scratch) {
+  using Store = typename StoreFor<Mech>::type;
+  Store S = make_store<Mech>(scratch, (Store*)nullptr);
+  const size_t n = (size_t)a.ncells;
+  const size_t T = (size_t)gridDim.x * kBlock;
+  for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
+    if (a.status && a.status[c] != CELL_SUCCESS) continue;
+    load_state<Mech>(a.conc, c, n, S);
+    const KTable k{a.ktab + c, n};
+    int nacc, nrej;
+    const int status = integrate_cell<Mech>(S, k, a, c, nacc, nrej);
+    store_state<Mech>(a.conc, c, n, S);
+    if (a.status) a.status[c] = status;
+    if (a.n_accept) a.n_accept[c] = nacc;
+    if (a.n_reject) a.n_reject[c] = nrej;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form: a grid sized to the SMs; every lane pulls cells from a
+// device work counter and refills itself as soon as its cell has finished,
+// so a warp's lanes stay busy even when cells need very different numbers
+// of attempts.  All lanes run the same attempt code on different cells.
+// ---------------------------------------------------------------------------
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 1) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
+  using Store = typename StoreFor<Mech>::type;
+  Store S = make_store<Mech>(scratch, (Store*)nullptr);
+  const size_t n = (size_t)a.ncells;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  long long cell = -1;       // -1: needs work; >= n: queue exhausted
+  int step = 0, status = CELL_SUCCESS, nacc = 0, nrej = 0;
+  bool flagged = false;      // cell rejected by the input checks: leave it untouched
+  Controller ctl;
+  ctl.start(a.dt, a.seed);
+  for (;;) {
+    const bool need = cell < 0;
+    const unsigned want = __ballot_sync(0xffffffffu, need);
+    if (want) {
+      const int leader = __ffs(want) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(a.queue, (unsigned)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        cell = (long long)base + __popc(want & lt_mask);
+        if (cell < (long long)n) {
+          status = a.status ? a.status[cell] : CELL_SUCCESS;
+          flagged = status != CELL_SUCCESS;
+          step = 0;
+          nacc = nrej = 0;
+          if (status == CELL_SUCCESS) load_state<Mech>(a.conc, (size_t)cell, n, S);
+          ctl.start(a.dt, a.seed);
+        }
+      }
+    }
+    const bool active = cell >= 0 && cell < (long long)n;
+    if (__ballot_sync(0xffffffffu, active) == 0u) break;
+    if (!active) continue;
+    bool done = status != CELL_SUCCESS;
+    if (!done) {
+      if (ctl.attempts >= a.max_attempts) {
+        status = CELL_ERR_CONVERGENCE_FAILURE;
+        done = true;
+      } else {
+        const KTable k{a.ktab + cell, n};
+        const double h = ctl.next_h();
+        int st = 0;
+        const double err = Mech::attempt(S, k, h, st);
+        if (st) status = CELL_ERR_SINGULAR_MATRIX;
+        if (ctl.update<Mech>(err)) {
+          apply_increment<Mech>(S);
+          ++nacc;
+        } else {
+          ++nrej;
+        }
+        if (!ctl.running()) {
+          if (++step < a.steps && status == CELL_SUCCESS) ctl.start(a.dt, a.seed);
+          else done = true;
+        }
+        if (status != CELL_SUCCESS) done = true;
+      }
+    }
+    if (done) {
+      const size_t cc = (size_t)cell;
+      if (!flagged) {
+        if (status == CELL_SUCCESS && !state_finite<Mech>(S)) status = CELL_ERR_NUMERICAL_FAILURE;
+        store_state<Mech>(a.conc, cc, n, S);
+        if (a.status) a.status[cc] = status;
+        if (a.n_accept) a.n_accept[cc] = nacc;
+        if (a.n_reject) a.n_reject[cc] = nrej;
+      }
+      cell = -1;
+    }
+  }
+}
+
+}  // namespace mkpp

@@ -1,0 +1,475 @@
+"""CUDA (sm_103a) emitter: plan JSON -> per-mechanism device header.
+
+The emitted header defines ``struct Mech`` in ``namespace mkpp_<name>`` with
+the per-cell arithmetic of one Rosenbrock attempt, fully unrolled, in FP64:
+
+* ``rate_constants``  - the reaction rate constants k_r(T, rho, fixed species,
+  runtime parameters), evaluated once per cell and host step instead of inside
+  every F/J expression (the reference inlines them,
+  ``src/mkpp/templates/device_impl/rates.hpp.j2:9-35``);
+* ``fun``             - mass-action F_i = sum_r net_ir * k_r * prod C^nu;
+* ``jac_w``           - W = I/(gamma h) - J written straight into the LU slots
+  (``integrate.j2:103-107``), J from the per-reaction partial derivatives;
+* ``factor``          - the row-wise Doolittle schedule of ``compact_plan``
+  (``src/mkpp/compact_plan.py:30-47``, executed by
+  ``device_impl/supernodal_factorize.hpp.j2:10-31``) unrolled with constant
+  slot indices, in place; each pivot is inverted once and the L entries of its
+  column are scaled by the reciprocal;
+* ``solve``           - forward (unit L) and backward substitution in the
+  order of ``device_impl/supernodal_solve.hpp.j2:10-42``;
+* ``attempt``         - the tableau stages, the increment sum M.K and the WRMS
+  error norm of ``integrate.j2:144-322``.
+
+The step controller and the kernels that drive it are mechanism independent
+and live in ``csrc/solver.cuh``.
+"""
+
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+from .plan import ReducedPlan, load
+
+GEN_DIR = Path(__file__).resolve().parent.parent / "generated"
+
+
+def _lit(x: float) -> str:
+    """Exact C literal for a double (17 significant digits, like ``%.17g``)."""
+    s = "%.17g" % float(x)
+    if "e" not in s and "." not in s and "n" not in s:
+        s += ".0"
+    return s
+
+
+def _k_text(expr: str) -> str:
+    expr = re.sub(r"\bP\[(\d+)\]", r"P(\1)", expr)
+    expr = re.sub(r"\bFIX\[(\d+)\]", r"FIX(\1)", expr)
+    return expr
+
+
+class _Code:
+    def __init__(self):
+        self.lines: list[str] = []
+
+    def __call__(self, s: str = ""):
+        self.lines.append(s)
+
+    def text(self) -> str:
+        return "\n".join(self.lines) + "\n"
+
+
+def _monomial(terms: list[tuple[int, int]], yname: str, v2l: dict[int, int]) -> list[str]:
+    """Factors of prod y^nu for (physical species, power) pairs, logical indices."""
+    fac = []
+    for s, pw in terms:
+        for _ in range(pw):
+            fac.append(f"{yname}[{v2l[s]}]")
+    return fac
+
+
+def _accumulate(target: str, init: str | None, terms: list[tuple[float, str]]) -> str:
+    """Sum ``init + c1*t1 + c2*t2 ...`` left to right, exact signs for +-1."""
+    expr = init
+    for c, t in terms:
+        if expr is None:
+            if c == 1.0:
+                expr = t
+            elif c == -1.0:
+                expr = f"-{t}"
+            else:
+                expr = f"{_lit(c)} * {t}"
+            continue
+        if c == 1.0:
+            expr = f"{expr} + {t}"
+        elif c == -1.0:
+            expr = f"{expr} - {t}"
+        else:
+            expr = f"fma({_lit(c)}, {t}, {expr})"
+    if expr is None:
+        expr = "0.0"
+    return f"{target} = {expr};"
+
+
+def _sum_expr(init: str | None, terms: list[tuple[float, str]]) -> str:
+    """Expression ``init + c1*t1 + c2*t2 ...`` accumulated left to right."""
+    return _accumulate("@", init, terms)[4:-1]
+
+
+def emit_mechanism(plan: ReducedPlan) -> str:
+    raw = plan.raw
+    name = plan.name
+    nv, ns, nr = plan.n_var, plan.n_species, len(plan.reactions)
+    v2l = plan.phys_to_var
+    tab = plan.tableau
+    stages = int(tab["stages"])
+    A, C, M, E, NewF = tab["A"], tab["C"], tab["M"], tab["E"], tab["NewF"]
+    gamma0 = tab["Gamma"][0]
+    elo = float(tab["ELO"])
+    nlu = len(plan.lu_slots)
+    np_ = max(1, plan.num_rate_parameters)
+    nfix = len(plan.fixed_phys)
+    c = _Code()
+    c(f"// Generated by mkpp_gb300.emitter.cuda_emitter from mechanisms/{name}.plan.json.")
+    c("// Do not edit: regenerate with `python -m mkpp_gb300.emitter.cuda_emitter`.")
+    c(f"// {ns} species ({nv} variable), {nr} reactions, {len(plan.w_slots)} W slots, "
+      f"{nlu} LU slots, {plan.lu_fma} LU products, {plan.lu_div} pivot scalings.")
+    c("#pragma once")
+    c('#include "mkpp_device.cuh"')
+    c(f"namespace mkpp_{name} {{")
+    c("")
+    c("struct Mech {")
+    c(f'  static constexpr const char* NAME = "{name}";')
+    c(f"  static constexpr int NS = {ns};      // species including fixed ones")
+    c(f"  static constexpr int NV = {nv};      // variable species (solved system)")
+    c(f"  static constexpr int NR = {nr};      // reactions")
+    c(f"  static constexpr int NP = {plan.num_rate_parameters};      // runtime parameter slots per cell")
+    c(f"  static constexpr int NPH = {plan.num_photolysis};      // photolysis slots")
+    c(f"  static constexpr int NFIX = {nfix};")
+    c(f"  static constexpr int NLU = {nlu};")
+    c(f"  static constexpr int NSTAGE = {stages};")
+    c(f"  static constexpr bool RUNTIME_ENV = {'true' if plan.runtime_environment else 'false'};")
+    c(f"  static constexpr bool CLOUD_GATED = {'true' if plan.cloud_gated else 'false'};")
+    c(f"  static constexpr double GAMMA = {_lit(gamma0)};")
+    c(f"  static constexpr double ELO = {_lit(elo)};")
+    c(f"  static constexpr double SEED = {_lit(plan.seed)};")
+    c(f"  static constexpr double ENV_T = {_lit(raw['environment_temperature'])};")
+    c(f"  static constexpr double ENV_RHO = {_lit(raw['environment_air_density'])};")
+    c(f"  static constexpr long long LU_FMA = {plan.lu_fma};")
+    c(f"  static constexpr long long LU_SCALE = {plan.lu_div};")
+    low, up = plan.solve_entries
+    c(f"  static constexpr long long SOLVE_L = {low};")
+    c(f"  static constexpr long long SOLVE_U = {up};")
+    # per-attempt algorithmic FP64 flop count (documented in the design doc)
+    fun_fl = sum(max(0, sum(pw for _, pw in r.reactants)) for r in plan.reactions) + \
+        sum(2 * len(r.net) for r in plan.reactions)
+    jac_fl = sum(2 * len(r.net) * len(r.reactants) for r in plan.reactions) + \
+        sum(len(r.reactants) * max(0, sum(pw for _, pw in r.reactants) - 1) for r in plan.reactions)
+    c(f"  static constexpr long long FUN_FLOPS = {fun_fl};")
+    c(f"  static constexpr long long JAC_FLOPS = {jac_fl};")
+    c("")
+    # physical index tables
+    c(f"  __host__ __device__ static constexpr int var_phys(int i) {{ constexpr int t[{nv}] = {{"
+      + ", ".join(str(x) for x in plan.var_phys) + "}; return t[i]; }")
+    if nfix:
+        c(f"  __host__ __device__ static constexpr int fix_phys(int i) {{ constexpr int t[{nfix}] = {{"
+          + ", ".join(str(x) for x in plan.fixed_phys) + "}; return t[i]; }")
+    else:
+        c("  __host__ __device__ static constexpr int fix_phys(int) { return 0; }")
+    c(f"  __host__ __device__ static constexpr double atol_v(int i) {{ constexpr double t[{nv}] = {{"
+      + ", ".join(_lit(plan.atol[p]) for p in plan.var_phys) + "}; return t[i]; }")
+    c(f"  __host__ __device__ static constexpr double rtol_v(int i) {{ constexpr double t[{nv}] = {{"
+      + ", ".join(_lit(plan.rtol[p]) for p in plan.var_phys) + "}; return t[i]; }")
+    c(f"  __host__ __device__ static constexpr int lu_prow(int s) {{ constexpr int t[{nlu}] = {{"
+      + ", ".join(str(plan.var_phys[r]) for r, _ in plan.lu_slots) + "}; return t[s]; }")
+    c(f"  __host__ __device__ static constexpr int lu_pcol(int s) {{ constexpr int t[{nlu}] = {{"
+      + ", ".join(str(plan.var_phys[cc]) for _, cc in plan.lu_slots) + "}; return t[s]; }")
+    names = ", ".join('"%s"' % x for x in raw["species"])
+    c(f"  static const char* species_name(int s) {{ static const char* t[{ns}] = {{{names}}}; return t[s]; }}")
+    # The reference names photolysis slots J_1..J_n (mkpp_c_api.cpp.j2:33-38).
+    if plan.num_photolysis:
+        pnames = ", ".join('"J_%d"' % (i + 1) for i in range(plan.num_photolysis))
+        c(f"  static const char* photolysis_name(int p) {{ static const char* t[{plan.num_photolysis}] = {{{pnames}}}; return t[p]; }}")
+    else:
+        c('  static const char* photolysis_name(int) { return ""; }')
+    c("")
+    # ---------------- rate constants
+    c("  // Rate constants of every reaction (reaction index order).  P(n) is the")
+    c("  // cell's runtime parameter n (photolysis J_n or external Rate slot n),")
+    c("  // FIX(s) the concentration of fixed species s, T/RHO the cell's")
+    c("  // temperature and air density.")
+    c("  template <class PA, class FA, class KO>")
+    c("  __device__ __forceinline__ static void rate_constants(const PA& P, const FA& FIX, double T, double RHO,")
+    c("                                                      double RH, double CLW, KO& k) {")
+    c("    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX;")
+    for r in plan.reactions:
+        c(f"    k.set({r.index}, {_k_text(r.k)});")
+    c("  }")
+    c("")
+    # ---------------- storage layout
+    nlu_ = nlu
+    Y = nlu_
+    K0 = Y + nv
+    FS = K0 + stages * nv
+    DY = FS + nv
+    nslots = DY + nv
+    c("  // Per-cell working storage, in slots of one double: the LU factors, the")
+    c("  // state y, the stage vectors K_1..K_s, the tendency F and the increment dy.")
+    c(f"  static constexpr int Y = {Y};")
+    c(f"  static constexpr int K0 = {K0};")
+    c(f"  static constexpr int F = {FS};")
+    c(f"  static constexpr int DY = {DY};")
+    c(f"  static constexpr int NSLOTS = {nslots};")
+    c("")
+    # ---------------- Fun
+    used_y_f = sorted({v2l[s_] for r in plan.reactions for s_, _ in r.reactants})
+    c("  // Mass-action tendencies F(y) of the variable species (logical order):")
+    c("  // y(i) supplies the state, out(i, F_i) receives the result.")
+    c("  template <class YA, class KA, class FO>")
+    c("  __device__ __forceinline__ static void fun(const YA& y, const KA& k, FO&& out) {")
+    for i in used_y_f:
+        c(f"    const double y{i} = y({i});")
+    rate_name = {}
+    for r in plan.reactions:
+        fac = [f"y{v2l[s_]}" for s_, pw in r.reactants for _ in range(pw)]
+        term = " * ".join([f"k({r.index})"] + fac)
+        c(f"    const double q{r.index} = {term};")
+        rate_name[r.index] = f"q{r.index}"
+    contrib = {i: [] for i in range(nv)}
+    for r in plan.reactions:
+        for s_, coef in r.net:
+            contrib[v2l[s_]].append((coef, rate_name[r.index]))
+    for i in range(nv):
+        c(f"    out({i}, {_sum_expr(None, contrib[i])});")
+    c("  }")
+    c("")
+    # ---------------- Jacobian -> W in LU slots
+    c("  // W = I/(gamma h) - J(y) into the LU slots that hold W entries.")
+    c("  template <class YA, class KA, class SA>")
+    c("  __device__ __forceinline__ static void jac_w(const YA& y, const KA& k, double inv_g_dt, SA& S) {")
+    c("    (void)inv_g_dt;")
+    used_y_j = sorted({v2l[s2] for r in plan.reactions if len(r.reactants) > 1 or any(pw > 1 for _, pw in r.reactants)
+                       for s2, _ in r.reactants})
+    for i in used_y_j:
+        c(f"    const double y{i} = y({i});")
+    partial_names = {}
+    for r in plan.reactions:
+        terms = list(r.reactants)
+        for idx, (s_, pw) in enumerate(terms):
+            others = []
+            for jdx, (s2, pw2) in enumerate(terms):
+                if jdx == idx:
+                    if pw2 > 1:
+                        others.append(_lit(float(pw2)))
+                        others += [f"y{v2l[s2]}"] * (pw2 - 1)
+                else:
+                    others += [f"y{v2l[s2]}"] * pw2
+            term = " * ".join([f"k({r.index})"] + others)
+            nm = f"d{r.index}_{v2l[s_]}"
+            partial_names[(r.index, s_)] = nm
+            c(f"    const double {nm} = {term};")
+    wterms = {loc: [] for loc in plan.w_slots}
+    for r in plan.reactions:
+        for s_, coef in r.net:
+            for s2, _pw in r.reactants:
+                wterms[(v2l[s_], v2l[s2])].append((-coef, partial_names[(r.index, s2)]))
+    for loc in plan.w_slots:
+        slot = plan.lu_index[loc]
+        init = "inv_g_dt" if loc[0] == loc[1] else None
+        c("    " + _accumulate(f"S[{slot}]", init, wterms[loc]))
+    c("  }")
+    c("")
+    c("  // Physical (row, column) of every W slot, for the dense Jacobian.")
+    c("  template <class Fn>")
+    c("  __device__ __forceinline__ static void for_each_w_slot(Fn&& fn) {")
+    for loc in plan.w_slots:
+        c(f"    fn({plan.lu_index[loc]}, {plan.var_phys[loc[0]]}, {plan.var_phys[loc[1]]});")
+    c("  }")
+    c("")
+    # ---------------- dense Jacobian: fixed-species columns
+    c("  // Fixed-species columns of the dense Jacobian: dF_i/dC_f through the")
+    c("  // rate constants' dependence on fixed species (third bodies).")
+    c("  template <class PA, class FA, class YA, class Fn>")
+    c("  __device__ __forceinline__ static void jac_fixed_columns(const PA& P, const FA& FIX, double T, double RHO,")
+    c("                                                         double RH, double CLW, const YA& y, Fn&& fn) {")
+    c("    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX; (void)y;")
+    colterms: dict = {}
+    for r, rr in zip(plan.reactions, raw["reactions"]):
+        for fidx, dexpr in rr.get("dk_dfixed", []):
+            mono = " * ".join(["(" + _k_text(dexpr) + ")"] + [f"y({v2l[s_]})" for s_, pw in r.reactants for _ in range(pw)])
+            for s_, coef in r.net:
+                colterms.setdefault((s_, fidx), []).append((coef, mono))
+    for (row, col), terms in sorted(colterms.items()):
+        c(f"    fn({row}, {col}, {_sum_expr(None, [(cf, '(' + t + ')') for cf, t in terms])});")
+    c("  }")
+    c("")
+    # ---------------- LU factorization
+    c("  // In-place row-wise Doolittle LU over the compact slots, in the operation")
+    c("  // order of the reference plan.  The operands a row reuses (its own L")
+    c("  // entries for the U part, the pivot column of U for the L part) are read")
+    c("  // once into registers.  Diagonal slots end up holding 1/U_ii.")
+    c("  template <class SA>")
+    c("  __device__ __forceinline__ static bool factor(SA& S) {")
+    c("    bool ok = true;")
+    diag_slots = set(plan.diag)
+    slot_rc = plan.lu_slots
+    # group ops by pivot row: U part (row == i) then L part (column == i)
+    i_cur = None
+    pre = {}
+    def row_of(op):
+        r, col = slot_rc[op[0]]
+        return min(r, col)
+    ops = plan.ops
+    idx = 0
+    while idx < len(ops):
+        i = row_of(ops[idx])
+        group = []
+        while idx < len(ops) and row_of(ops[idx]) == i:
+            group.append(ops[idx])
+            idx += 1
+        upart = [o for o in group if slot_rc[o[0]][0] == i]
+        lpart = [o for o in group if slot_rc[o[0]][0] != i]
+        c(f"    {{  // pivot row {i}")
+        # preload the row's L entries used by the U part
+        lslots = sorted({plan.products[q][0] for o in upart for q in range(o[2], o[3])})
+        for sl in lslots:
+            c(f"      const double a{sl} = S[{sl}];")
+        rd = None
+        for out, w, b, e, dg in upart:
+            expr = f"S[{out}]" if w >= 0 else "0.0"
+            for q in range(b, e):
+                l_, u_ = plan.products[q]
+                expr = f"fma(-a{l_}, S[{u_}], {expr})"
+            if out in diag_slots:
+                c(f"      const double u{out} = {expr};")
+                c(f"      ok = ok && (u{out} != 0.0);")
+                c(f"      const double rd = 1.0 / u{out};")
+                c(f"      S[{out}] = rd;")
+                rd = "rd"
+            elif expr != f"S[{out}]":
+                c(f"      S[{out}] = {expr};")
+        uslots = sorted({plan.products[q][1] for o in lpart for q in range(o[2], o[3])})
+        for sl in uslots:
+            c(f"      const double b{sl} = S[{sl}];")
+        for out, w, b, e, dg in lpart:
+            expr = f"S[{out}]" if w >= 0 else "0.0"
+            for q in range(b, e):
+                l_, u_ = plan.products[q]
+                expr = f"fma(-S[{l_}], b{u_}, {expr})"
+            c(f"      S[{out}] = ({expr}) * rd;")
+        c("    }")
+    c("    return ok;")
+    c("  }")
+    c("")
+    # ---------------- Solve
+    c("  // Solve (LU) x = b in place on slots [base, base + NV): unit-L forward")
+    c("  // sweep, then the U backward sweep scaled by the stored 1/U_ii.")
+    c("  template <class SA>")
+    c("  __device__ __forceinline__ static void solve(SA& S, const int base) {")
+    for i in range(nv):
+        expr = f"S[base + {i}]"
+        for col, slot in plan.lower[i]:
+            expr = f"fma(-S[{slot}], v{col}, {expr})"
+        c(f"    const double v{i} = {expr};")
+    for i in range(nv - 1, -1, -1):
+        expr = f"v{i}"
+        for col, slot in plan.upper[i]:
+            expr = f"fma(-S[{slot}], x{col}, {expr})"
+        c(f"    const double x{i} = ({expr}) * S[{plan.diag[i]}];")
+        c(f"    S[base + {i}] = x{i};")
+    c("  }")
+    c("")
+    # ---------------- Attempt
+    c("  // One Rosenbrock attempt of size h from the state in S[Y..].  Returns the")
+    c("  // WRMS error norm and leaves the increment sum_j M_j K_j in S[DY..].")
+    c("  // Bit 1 of status is set on a zero pivot.")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static double attempt(SA& S, const KA& k, double h, int& status) {")
+    c("    const double inv_g_dt = 1.0 / (GAMMA * h);")
+    c("    jac_w([&](int i) { return S[Y + i]; }, k, inv_g_dt, S);")
+    c("    if (!factor(S)) status |= 1;")
+    for st in range(1, stages + 1):
+        kb = K0 + (st - 1) * nv
+        if NewF[st - 1]:
+            if st == 1:
+                c("    fun([&](int i) { return S[Y + i]; }, k, [&](int i, double v) { S[F + i] = v; });")
+            else:
+                terms = []
+                for j in range(1, st):
+                    a = A[(st - 1) * (st - 2) // 2 + j - 1]
+                    if a != 0.0:
+                        terms.append((a, j))
+                expr = "S[Y + i]"
+                for a, j in terms:
+                    kk = f"S[{K0 + (j - 1) * nv} + i]"
+                    expr = f"{expr} + {kk}" if a == 1.0 else f"{expr} + {_lit(a)} * {kk}"
+                c(f"    fun([&](int i) {{ return {expr}; }}, k, [&](int i, double v) {{ S[F + i] = v; }});")
+        cterms = []
+        if st > 1:
+            for j in range(1, st):
+                cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+                if cv != 0.0:
+                    cterms.append((cv, j))
+        for cv, j in cterms:
+            c(f"    const double c{st}{j} = {_lit(cv)} / h;")
+        c("    #pragma unroll")
+        c("    for (int i = 0; i < NV; ++i) {")
+        expr = "S[F + i]"
+        for cv, j in cterms:
+            expr = f"fma(c{st}{j}, S[{K0 + (j - 1) * nv} + i], {expr})"
+        c(f"      S[{kb} + i] = {expr};")
+        c("    }")
+        c(f"    solve(S, {kb});")
+    c("    double err_sq = 0.0;")
+    c("    #pragma unroll")
+    c("    for (int i = 0; i < NV; ++i) {")
+    for j in range(stages):
+        c(f"      const double k{j} = S[{K0 + j * nv} + i];")
+    mterms = [(M[j], j) for j in range(stages) if M[j] != 0.0]
+    eterms = [(E[j], j) for j in range(stages) if E[j] != 0.0]
+
+    def lin(terms):
+        expr = None
+        for cv, j in terms:
+            t = f"k{j}"
+            if expr is None:
+                expr = t if cv == 1.0 else f"{_lit(cv)} * {t}"
+            else:
+                expr = f"{expr} + {t}" if cv == 1.0 else f"fma({_lit(cv)}, {t}, {expr})"
+        return expr or "0.0"
+
+    # Ynew = ((S + K1) + M2 K2) + ... (integrate.j2 error block); the accepted
+    # increment is K1 + M2 K2 + ... (integrate.j2 accept block).
+    c("      const double yi = S[Y + i];")
+    ynew = "yi"
+    for cv, j in mterms:
+        ynew = f"{ynew} + k{j}" if cv == 1.0 else f"fma({_lit(cv)}, k{j}, {ynew})"
+    c(f"      const double ynew = {ynew};")
+    c(f"      S[DY + i] = {lin(mterms)};")
+    c("      const double sc = fma(rtol_v(i), fmax(fabs(yi), fabs(ynew)), atol_v(i));")
+    c(f"      const double q = ({lin(eterms)}) / sc;")
+    c("      err_sq = fma(q, q, err_sq);")
+    c("    }")
+    c(f"    return fmax(sqrt(err_sq / {ns}.0), 1.0e-10);")
+    c("  }")
+    c("")
+    c("  // Step-size factor from the error norm (integrate.j2:324-333).")
+    c("  __device__ __forceinline__ static double growth(double err) {")
+    if elo == 2.0:
+        c("    const double fac = 0.9 / sqrt(err);")
+    elif elo == 3.0:
+        c("    const double fac = 0.9 / cbrt(err);")
+    else:
+        c(f"    const double fac = 0.9 * pow(err, -{_lit(1.0 / elo)});")
+    c("    return fmax(0.2, fmin(fac, 6.0));")
+    c("  }")
+    c("};")
+    c("")
+    c(f"}}  // namespace mkpp_{name}")
+    return c.text()
+
+
+def write(name: str, out_dir: Path = GEN_DIR) -> Path:
+    plan = load(name)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    path = out_dir / f"{name}.cuh"
+    text = emit_mechanism(plan)
+    if not path.exists() or path.read_text() != text:
+        path.write_text(text)
+    return path
+
+
+def main(argv=None) -> int:
+    import argparse
+
+    ap = argparse.ArgumentParser(description="Emit sm_103a device headers from plan JSON")
+    ap.add_argument("mechanisms", nargs="*", default=["chapman", "small_strato", "saprc99"])
+    args = ap.parse_args(argv)
+    for m in args.mechanisms:
+        p = write(m)
+        print(f"{m} -> {p} ({p.stat().st_size // 1024} KiB)")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

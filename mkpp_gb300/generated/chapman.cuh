@@ -1,0 +1,230 @@
+// Generated by mkpp_gb300.emitter.cuda_emitter from mechanisms/chapman.plan.json.
+// Do not edit: regenerate with `python -m mkpp_gb300.emitter.cuda_emitter`.
+// 4 species (3 variable), 4 reactions, 9 W slots, 9 LU slots, 5 LU products, 3 pivot scalings.
+#pragma once
+#include "mkpp_device.cuh"
+namespace mkpp_chapman {
+
+struct Mech {
+  static constexpr const char* NAME = "chapman";
+  static constexpr int NS = 4;      // species including fixed ones
+  static constexpr int NV = 3;      // variable species (solved system)
+  static constexpr int NR = 4;      // reactions
+  static constexpr int NP = 2;      // runtime parameter slots per cell
+  static constexpr int NPH = 2;      // photolysis slots
+  static constexpr int NFIX = 1;
+  static constexpr int NLU = 9;
+  static constexpr int NSTAGE = 3;
+  static constexpr bool RUNTIME_ENV = false;
+  static constexpr bool CLOUD_GATED = false;
+  static constexpr double GAMMA = 0.435866521508459;
+  static constexpr double ELO = 3.0;
+  static constexpr double SEED = 9.9999999999999995e-07;
+  static constexpr double ENV_T = 298.14999999999998;
+  static constexpr double ENV_RHO = 2.46e+19;
+  static constexpr long long LU_FMA = 5;
+  static constexpr long long LU_SCALE = 3;
+  static constexpr long long SOLVE_L = 3;
+  static constexpr long long SOLVE_U = 3;
+  static constexpr long long FUN_FLOPS = 28;
+  static constexpr long long JAC_FLOPS = 38;
+
+  __host__ __device__ static constexpr int var_phys(int i) { constexpr int t[3] = {2, 0, 1}; return t[i]; }
+  __host__ __device__ static constexpr int fix_phys(int i) { constexpr int t[1] = {3}; return t[i]; }
+  __host__ __device__ static constexpr double atol_v(int i) { constexpr double t[3] = {1.0, 1.0, 1.0}; return t[i]; }
+  __host__ __device__ static constexpr double rtol_v(int i) { constexpr double t[3] = {0.001, 0.001, 0.001}; return t[i]; }
+  __host__ __device__ static constexpr int lu_prow(int s) { constexpr int t[9] = {2, 2, 2, 0, 0, 0, 1, 1, 1}; return t[s]; }
+  __host__ __device__ static constexpr int lu_pcol(int s) { constexpr int t[9] = {2, 0, 1, 2, 0, 1, 2, 0, 1}; return t[s]; }
+  static const char* species_name(int s) { static const char* t[4] = {"O", "O2", "O3", "M"}; return t[s]; }
+  static const char* photolysis_name(int p) { static const char* t[2] = {"J_1", "J_2"}; return t[p]; }
+
+  // Rate constants of every reaction (reaction index order).  P(n) is the
+  // cell's runtime parameter n (photolysis J_n or external Rate slot n),
+  // FIX(s) the concentration of fixed species s, T/RHO the cell's
+  // temperature and air density.
+  template <class PA, class FA, class KO>
+  __device__ __forceinline__ static void rate_constants(const PA& P, const FA& FIX, double T, double RHO,
+                                                      double RH, double CLW, KO& k) {
+    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX;
+    k.set(0, P(0));
+    k.set(1, 6.0e-34*FIX(3));
+    k.set(2, P(1));
+    k.set(3, 7.9999999999999998e-12);
+  }
+
+  // Per-cell working storage, in slots of one double: the LU factors, the
+  // state y, the stage vectors K_1..K_s, the tendency F and the increment dy.
+  static constexpr int Y = 9;
+  static constexpr int K0 = 12;
+  static constexpr int F = 21;
+  static constexpr int DY = 24;
+  static constexpr int NSLOTS = 27;
+
+  // Mass-action tendencies F(y) of the variable species (logical order):
+  // y(i) supplies the state, out(i, F_i) receives the result.
+  template <class YA, class KA, class FO>
+  __device__ __forceinline__ static void fun(const YA& y, const KA& k, FO&& out) {
+    const double y0 = y(0);
+    const double y1 = y(1);
+    const double y2 = y(2);
+    const double q0 = k(0) * y2;
+    const double q1 = k(1) * y1 * y2;
+    const double q2 = k(2) * y0;
+    const double q3 = k(3) * y1 * y0;
+    out(0, q1 - q2 - q3);
+    out(1, 2.0 * q0 - q1 + q2 - q3);
+    out(2, fma(2.0, q3, -q0 - q1 + q2));
+  }
+
+  // W = I/(gamma h) - J(y) into the LU slots that hold W entries.
+  template <class YA, class KA, class SA>
+  __device__ __forceinline__ static void jac_w(const YA& y, const KA& k, double inv_g_dt, SA& S) {
+    (void)inv_g_dt;
+    const double y0 = y(0);
+    const double y1 = y(1);
+    const double y2 = y(2);
+    const double d0_2 = k(0);
+    const double d1_1 = k(1) * y2;
+    const double d1_2 = k(1) * y1;
+    const double d2_0 = k(2);
+    const double d3_1 = k(3) * y0;
+    const double d3_0 = k(3) * y1;
+    S[0] = inv_g_dt + d2_0 + d3_0;
+    S[1] = -d1_1 + d3_1;
+    S[2] = -d1_2;
+    S[3] = -d2_0 + d3_0;
+    S[4] = inv_g_dt + d1_1 + d3_1;
+    S[5] = -2.0 * d0_2 + d1_2;
+    S[6] = fma(-2.0, d3_0, -d2_0);
+    S[7] = fma(-2.0, d3_1, d1_1);
+    S[8] = inv_g_dt + d0_2 + d1_2;
+  }
+
+  // Physical (row, column) of every W slot, for the dense Jacobian.
+  template <class Fn>
+  __device__ __forceinline__ static void for_each_w_slot(Fn&& fn) {
+    fn(0, 2, 2);
+    fn(1, 2, 0);
+    fn(2, 2, 1);
+    fn(3, 0, 2);
+    fn(4, 0, 0);
+    fn(5, 0, 1);
+    fn(6, 1, 2);
+    fn(7, 1, 0);
+    fn(8, 1, 1);
+  }
+
+  // Fixed-species columns of the dense Jacobian: dF_i/dC_f through the
+  // rate constants' dependence on fixed species (third bodies).
+  template <class PA, class FA, class YA, class Fn>
+  __device__ __forceinline__ static void jac_fixed_columns(const PA& P, const FA& FIX, double T, double RHO,
+                                                         double RH, double CLW, const YA& y, Fn&& fn) {
+    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX; (void)y;
+    fn(0, 3, -((6.0e-34) * y(1) * y(2)));
+    fn(1, 3, -((6.0e-34) * y(1) * y(2)));
+    fn(2, 3, ((6.0e-34) * y(1) * y(2)));
+  }
+
+  // In-place row-wise Doolittle LU over the compact slots, in the operation
+  // order of the reference plan.  The operands a row reuses (its own L
+  // entries for the U part, the pivot column of U for the L part) are read
+  // once into registers.  Diagonal slots end up holding 1/U_ii.
+  template <class SA>
+  __device__ __forceinline__ static bool factor(SA& S) {
+    bool ok = true;
+    {  // pivot row 0
+      const double u0 = S[0];
+      ok = ok && (u0 != 0.0);
+      const double rd = 1.0 / u0;
+      S[0] = rd;
+      S[3] = (S[3]) * rd;
+      S[6] = (S[6]) * rd;
+    }
+    {  // pivot row 1
+      const double a3 = S[3];
+      const double u4 = fma(-a3, S[1], S[4]);
+      ok = ok && (u4 != 0.0);
+      const double rd = 1.0 / u4;
+      S[4] = rd;
+      S[5] = fma(-a3, S[2], S[5]);
+      const double b1 = S[1];
+      S[7] = (fma(-S[6], b1, S[7])) * rd;
+    }
+    {  // pivot row 2
+      const double a6 = S[6];
+      const double a7 = S[7];
+      const double u8 = fma(-a7, S[5], fma(-a6, S[2], S[8]));
+      ok = ok && (u8 != 0.0);
+      const double rd = 1.0 / u8;
+      S[8] = rd;
+    }
+    return ok;
+  }
+
+  // Solve (LU) x = b in place on slots [base, base + NV): unit-L forward
+  // sweep, then the U backward sweep scaled by the stored 1/U_ii.
+  template <class SA>
+  __device__ __forceinline__ static void solve(SA& S, const int base) {
+    const double v0 = S[base + 0];
+    const double v1 = fma(-S[3], v0, S[base + 1]);
+    const double v2 = fma(-S[7], v1, fma(-S[6], v0, S[base + 2]));
+    const double x2 = (v2) * S[8];
+    S[base + 2] = x2;
+    const double x1 = (fma(-S[5], x2, v1)) * S[4];
+    S[base + 1] = x1;
+    const double x0 = (fma(-S[2], x2, fma(-S[1], x1, v0))) * S[0];
+    S[base + 0] = x0;
+  }
+
+  // One Rosenbrock attempt of size h from the state in S[Y..].  Returns the
+  // WRMS error norm and leaves the increment sum_j M_j K_j in S[DY..].
+  // Bit 1 of status is set on a zero pivot.
+  template <class SA, class KA>
+  __device__ __forceinline__ static double attempt(SA& S, const KA& k, double h, int& status) {
+    const double inv_g_dt = 1.0 / (GAMMA * h);
+    jac_w([&](int i) { return S[Y + i]; }, k, inv_g_dt, S);
+    if (!factor(S)) status |= 1;
+    fun([&](int i) { return S[Y + i]; }, k, [&](int i, double v) { S[F + i] = v; });
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[12 + i] = S[F + i];
+    }
+    solve(S, 12);
+    fun([&](int i) { return S[Y + i] + S[12 + i]; }, k, [&](int i, double v) { S[F + i] = v; });
+    const double c21 = -1.0156171083877703 / h;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[15 + i] = fma(c21, S[12 + i], S[F + i]);
+    }
+    solve(S, 15);
+    const double c31 = 4.0759956452537702 / h;
+    const double c32 = 9.20767942983308 / h;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[18 + i] = fma(c32, S[15 + i], fma(c31, S[12 + i], S[F + i]));
+    }
+    solve(S, 18);
+    double err_sq = 0.0;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      const double k0 = S[12 + i];
+      const double k1 = S[15 + i];
+      const double k2 = S[18 + i];
+      const double yi = S[Y + i];
+      const double ynew = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, yi + k0));
+      S[DY + i] = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, k0));
+      const double sc = fma(rtol_v(i), fmax(fabs(yi), fabs(ynew)), atol_v(i));
+      const double q = (fma(0.22354069897811571, k2, fma(-2.9079558716805471, k1, 0.5 * k0))) / sc;
+      err_sq = fma(q, q, err_sq);
+    }
+    return fmax(sqrt(err_sq / 4.0), 1.0e-10);
+  }
+
+  // Step-size factor from the error norm (integrate.j2:324-333).
+  __device__ __forceinline__ static double growth(double err) {
+    const double fac = 0.9 / cbrt(err);
+    return fmax(0.2, fmin(fac, 6.0));
+  }
+};
+
+}  // namespace mkpp_chapman

@@ -1,0 +1,349 @@
+// Generated by mkpp_gb300.emitter.cuda_emitter from mechanisms/small_strato.plan.json.
+// Do not edit: regenerate with `python -m mkpp_gb300.emitter.cuda_emitter`.
+// 7 species (6 variable), 10 reactions, 26 W slots, 29 LU slots, 29 LU products, 13 pivot scalings.
+#pragma once
+#include "mkpp_device.cuh"
+namespace mkpp_small_strato {
+
+struct Mech {
+  static constexpr const char* NAME = "small_strato";
+  static constexpr int NS = 7;      // species including fixed ones
+  static constexpr int NV = 6;      // variable species (solved system)
+  static constexpr int NR = 10;      // reactions
+  static constexpr int NP = 4;      // runtime parameter slots per cell
+  static constexpr int NPH = 4;      // photolysis slots
+  static constexpr int NFIX = 1;
+  static constexpr int NLU = 29;
+  static constexpr int NSTAGE = 3;
+  static constexpr bool RUNTIME_ENV = false;
+  static constexpr bool CLOUD_GATED = false;
+  static constexpr double GAMMA = 0.435866521508459;
+  static constexpr double ELO = 3.0;
+  static constexpr double SEED = 9.9999999999999995e-07;
+  static constexpr double ENV_T = 298.14999999999998;
+  static constexpr double ENV_RHO = 2.46e+19;
+  static constexpr long long LU_FMA = 29;
+  static constexpr long long LU_SCALE = 13;
+  static constexpr long long SOLVE_L = 13;
+  static constexpr long long SOLVE_U = 10;
+  static constexpr long long FUN_FLOPS = 75;
+  static constexpr long long JAC_FLOPS = 104;
+
+  __host__ __device__ static constexpr int var_phys(int i) { constexpr int t[6] = {1, 0, 6, 2, 3, 4}; return t[i]; }
+  __host__ __device__ static constexpr int fix_phys(int i) { constexpr int t[1] = {5}; return t[i]; }
+  __host__ __device__ static constexpr double atol_v(int i) { constexpr double t[6] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0}; return t[i]; }
+  __host__ __device__ static constexpr double rtol_v(int i) { constexpr double t[6] = {0.001, 0.001, 0.001, 0.001, 0.001, 0.001}; return t[i]; }
+  __host__ __device__ static constexpr int lu_prow(int s) { constexpr int t[29] = {1, 1, 0, 0, 0, 0, 0, 6, 6, 6, 6, 6, 6, 2, 2, 2, 2, 2, 2, 3, 3, 3, 3, 3, 4, 4, 4, 4, 4}; return t[s]; }
+  __host__ __device__ static constexpr int lu_pcol(int s) { constexpr int t[29] = {1, 2, 1, 0, 6, 2, 4, 1, 0, 6, 2, 3, 4, 1, 0, 6, 2, 3, 4, 0, 6, 2, 3, 4, 0, 6, 2, 3, 4}; return t[s]; }
+  static const char* species_name(int s) { static const char* t[7] = {"O", "O1D", "O3", "NO", "NO2", "M", "O2"}; return t[s]; }
+  static const char* photolysis_name(int p) { static const char* t[4] = {"J_1", "J_2", "J_3", "J_4"}; return t[p]; }
+
+  // Rate constants of every reaction (reaction index order).  P(n) is the
+  // cell's runtime parameter n (photolysis J_n or external Rate slot n),
+  // FIX(s) the concentration of fixed species s, T/RHO the cell's
+  // temperature and air density.
+  template <class PA, class FA, class KO>
+  __device__ __forceinline__ static void rate_constants(const PA& P, const FA& FIX, double T, double RHO,
+                                                      double RH, double CLW, KO& k) {
+    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX;
+    k.set(0, P(0));
+    k.set(1, 8.0180000000000003e-17);
+    k.set(2, P(1));
+    k.set(3, 1.576e-15);
+    k.set(4, P(2));
+    k.set(5, 7.1100000000000005e-11*FIX(5));
+    k.set(6, 1.2e-10);
+    k.set(7, 6.0620000000000003e-15);
+    k.set(8, 1.0690000000000001e-11);
+    k.set(9, P(3));
+  }
+
+  // Per-cell working storage, in slots of one double: the LU factors, the
+  // state y, the stage vectors K_1..K_s, the tendency F and the increment dy.
+  static constexpr int Y = 29;
+  static constexpr int K0 = 35;
+  static constexpr int F = 53;
+  static constexpr int DY = 59;
+  static constexpr int NSLOTS = 65;
+
+  // Mass-action tendencies F(y) of the variable species (logical order):
+  // y(i) supplies the state, out(i, F_i) receives the result.
+  template <class YA, class KA, class FO>
+  __device__ __forceinline__ static void fun(const YA& y, const KA& k, FO&& out) {
+    const double y0 = y(0);
+    const double y1 = y(1);
+    const double y2 = y(2);
+    const double y3 = y(3);
+    const double y4 = y(4);
+    const double y5 = y(5);
+    const double q0 = k(0) * y2;
+    const double q1 = k(1) * y1 * y2;
+    const double q2 = k(2) * y3;
+    const double q3 = k(3) * y1 * y3;
+    const double q4 = k(4) * y3;
+    const double q5 = k(5) * y0;
+    const double q6 = k(6) * y0 * y3;
+    const double q7 = k(7) * y4 * y3;
+    const double q8 = k(8) * y5 * y1;
+    const double q9 = k(9) * y5;
+    out(0, q4 - q5 - q6);
+    out(1, 2.0 * q0 - q1 + q2 - q3 + q5 - q8 + q9);
+    out(2, fma(2.0, q6, fma(2.0, q3, -q0 - q1 + q2) + q4) + q7 + q8);
+    out(3, q1 - q2 - q3 - q4 - q6 - q7);
+    out(4, -q7 + q8 + q9);
+    out(5, q7 - q8 - q9);
+  }
+
+  // W = I/(gamma h) - J(y) into the LU slots that hold W entries.
+  template <class YA, class KA, class SA>
+  __device__ __forceinline__ static void jac_w(const YA& y, const KA& k, double inv_g_dt, SA& S) {
+    (void)inv_g_dt;
+    const double y0 = y(0);
+    const double y1 = y(1);
+    const double y2 = y(2);
+    const double y3 = y(3);
+    const double y4 = y(4);
+    const double y5 = y(5);
+    const double d0_2 = k(0);
+    const double d1_1 = k(1) * y2;
+    const double d1_2 = k(1) * y1;
+    const double d2_3 = k(2);
+    const double d3_1 = k(3) * y3;
+    const double d3_3 = k(3) * y1;
+    const double d4_3 = k(4);
+    const double d5_0 = k(5);
+    const double d6_0 = k(6) * y3;
+    const double d6_3 = k(6) * y0;
+    const double d7_4 = k(7) * y3;
+    const double d7_3 = k(7) * y4;
+    const double d8_5 = k(8) * y1;
+    const double d8_1 = k(8) * y5;
+    const double d9_5 = k(9);
+    S[0] = inv_g_dt + d5_0 + d6_0;
+    S[1] = -d4_3 + d6_3;
+    S[2] = -d5_0;
+    S[3] = inv_g_dt + d1_1 + d3_1 + d8_1;
+    S[4] = -2.0 * d0_2 + d1_2;
+    S[5] = -d2_3 + d3_3;
+    S[6] = d8_5 - d9_5;
+    S[7] = -2.0 * d6_0;
+    S[8] = fma(-2.0, d3_1, d1_1) - d8_1;
+    S[9] = inv_g_dt + d0_2 + d1_2;
+    S[10] = fma(-2.0, d6_3, fma(-2.0, d3_3, -d2_3) - d4_3) - d7_3;
+    S[11] = -d7_4;
+    S[12] = -d8_5;
+    S[13] = d6_0;
+    S[14] = -d1_1 + d3_1;
+    S[15] = -d1_2;
+    S[16] = inv_g_dt + d2_3 + d3_3 + d4_3 + d6_3 + d7_3;
+    S[17] = d7_4;
+    S[19] = -d8_1;
+    S[21] = d7_3;
+    S[22] = inv_g_dt + d7_4;
+    S[23] = -d8_5 - d9_5;
+    S[24] = d8_1;
+    S[26] = -d7_3;
+    S[27] = -d7_4;
+    S[28] = inv_g_dt + d8_5 + d9_5;
+  }
+
+  // Physical (row, column) of every W slot, for the dense Jacobian.
+  template <class Fn>
+  __device__ __forceinline__ static void for_each_w_slot(Fn&& fn) {
+    fn(0, 1, 1);
+    fn(1, 1, 2);
+    fn(2, 0, 1);
+    fn(3, 0, 0);
+    fn(4, 0, 6);
+    fn(5, 0, 2);
+    fn(6, 0, 4);
+    fn(7, 6, 1);
+    fn(8, 6, 0);
+    fn(9, 6, 6);
+    fn(10, 6, 2);
+    fn(11, 6, 3);
+    fn(12, 6, 4);
+    fn(13, 2, 1);
+    fn(14, 2, 0);
+    fn(15, 2, 6);
+    fn(16, 2, 2);
+    fn(17, 2, 3);
+    fn(19, 3, 0);
+    fn(21, 3, 2);
+    fn(22, 3, 3);
+    fn(23, 3, 4);
+    fn(24, 4, 0);
+    fn(26, 4, 2);
+    fn(27, 4, 3);
+    fn(28, 4, 4);
+  }
+
+  // Fixed-species columns of the dense Jacobian: dF_i/dC_f through the
+  // rate constants' dependence on fixed species (third bodies).
+  template <class PA, class FA, class YA, class Fn>
+  __device__ __forceinline__ static void jac_fixed_columns(const PA& P, const FA& FIX, double T, double RHO,
+                                                         double RH, double CLW, const YA& y, Fn&& fn) {
+    (void)T; (void)RHO; (void)RH; (void)CLW; (void)P; (void)FIX; (void)y;
+    fn(0, 5, ((7.1100000000000005e-11) * y(0)));
+    fn(1, 5, -((7.1100000000000005e-11) * y(0)));
+  }
+
+  // In-place row-wise Doolittle LU over the compact slots, in the operation
+  // order of the reference plan.  The operands a row reuses (its own L
+  // entries for the U part, the pivot column of U for the L part) are read
+  // once into registers.  Diagonal slots end up holding 1/U_ii.
+  template <class SA>
+  __device__ __forceinline__ static bool factor(SA& S) {
+    bool ok = true;
+    {  // pivot row 0
+      const double u0 = S[0];
+      ok = ok && (u0 != 0.0);
+      const double rd = 1.0 / u0;
+      S[0] = rd;
+      S[2] = (S[2]) * rd;
+      S[7] = (S[7]) * rd;
+      S[13] = (S[13]) * rd;
+    }
+    {  // pivot row 1
+      const double a2 = S[2];
+      const double u3 = S[3];
+      ok = ok && (u3 != 0.0);
+      const double rd = 1.0 / u3;
+      S[3] = rd;
+      S[5] = fma(-a2, S[1], S[5]);
+      S[8] = (S[8]) * rd;
+      S[14] = (S[14]) * rd;
+      S[19] = (S[19]) * rd;
+      S[24] = (S[24]) * rd;
+    }
+    {  // pivot row 2
+      const double a7 = S[7];
+      const double a8 = S[8];
+      const double u9 = fma(-a8, S[4], S[9]);
+      ok = ok && (u9 != 0.0);
+      const double rd = 1.0 / u9;
+      S[9] = rd;
+      S[10] = fma(-a8, S[5], fma(-a7, S[1], S[10]));
+      S[12] = fma(-a8, S[6], S[12]);
+      const double b4 = S[4];
+      S[15] = (fma(-S[14], b4, S[15])) * rd;
+      S[20] = (fma(-S[19], b4, 0.0)) * rd;
+      S[25] = (fma(-S[24], b4, 0.0)) * rd;
+    }
+    {  // pivot row 3
+      const double a13 = S[13];
+      const double a14 = S[14];
+      const double a15 = S[15];
+      const double u16 = fma(-a15, S[10], fma(-a14, S[5], fma(-a13, S[1], S[16])));
+      ok = ok && (u16 != 0.0);
+      const double rd = 1.0 / u16;
+      S[16] = rd;
+      S[17] = fma(-a15, S[11], S[17]);
+      S[18] = fma(-a15, S[12], fma(-a14, S[6], 0.0));
+      const double b5 = S[5];
+      const double b10 = S[10];
+      S[21] = (fma(-S[20], b10, fma(-S[19], b5, S[21]))) * rd;
+      S[26] = (fma(-S[25], b10, fma(-S[24], b5, S[26]))) * rd;
+    }
+    {  // pivot row 4
+      const double a19 = S[19];
+      const double a20 = S[20];
+      const double a21 = S[21];
+      const double u22 = fma(-a21, S[17], fma(-a20, S[11], S[22]));
+      ok = ok && (u22 != 0.0);
+      const double rd = 1.0 / u22;
+      S[22] = rd;
+      S[23] = fma(-a21, S[18], fma(-a20, S[12], fma(-a19, S[6], S[23])));
+      const double b11 = S[11];
+      const double b17 = S[17];
+      S[27] = (fma(-S[26], b17, fma(-S[25], b11, S[27]))) * rd;
+    }
+    {  // pivot row 5
+      const double a24 = S[24];
+      const double a25 = S[25];
+      const double a26 = S[26];
+      const double a27 = S[27];
+      const double u28 = fma(-a27, S[23], fma(-a26, S[18], fma(-a25, S[12], fma(-a24, S[6], S[28]))));
+      ok = ok && (u28 != 0.0);
+      const double rd = 1.0 / u28;
+      S[28] = rd;
+    }
+    return ok;
+  }
+
+  // Solve (LU) x = b in place on slots [base, base + NV): unit-L forward
+  // sweep, then the U backward sweep scaled by the stored 1/U_ii.
+  template <class SA>
+  __device__ __forceinline__ static void solve(SA& S, const int base) {
+    const double v0 = S[base + 0];
+    const double v1 = fma(-S[2], v0, S[base + 1]);
+    const double v2 = fma(-S[8], v1, fma(-S[7], v0, S[base + 2]));
+    const double v3 = fma(-S[15], v2, fma(-S[14], v1, fma(-S[13], v0, S[base + 3])));
+    const double v4 = fma(-S[21], v3, fma(-S[20], v2, fma(-S[19], v1, S[base + 4])));
+    const double v5 = fma(-S[27], v4, fma(-S[26], v3, fma(-S[25], v2, fma(-S[24], v1, S[base + 5]))));
+    const double x5 = (v5) * S[28];
+    S[base + 5] = x5;
+    const double x4 = (fma(-S[23], x5, v4)) * S[22];
+    S[base + 4] = x4;
+    const double x3 = (fma(-S[18], x5, fma(-S[17], x4, v3))) * S[16];
+    S[base + 3] = x3;
+    const double x2 = (fma(-S[12], x5, fma(-S[11], x4, fma(-S[10], x3, v2)))) * S[9];
+    S[base + 2] = x2;
+    const double x1 = (fma(-S[6], x5, fma(-S[5], x3, fma(-S[4], x2, v1)))) * S[3];
+    S[base + 1] = x1;
+    const double x0 = (fma(-S[1], x3, v0)) * S[0];
+    S[base + 0] = x0;
+  }
+
+  // One Rosenbrock attempt of size h from the state in S[Y..].  Returns the
+  // WRMS error norm and leaves the increment sum_j M_j K_j in S[DY..].
+  // Bit 1 of status is set on a zero pivot.
+  template <class SA, class KA>
+  __device__ __forceinline__ static double attempt(SA& S, const KA& k, double h, int& status) {
+    const double inv_g_dt = 1.0 / (GAMMA * h);
+    jac_w([&](int i) { return S[Y + i]; }, k, inv_g_dt, S);
+    if (!factor(S)) status |= 1;
+    fun([&](int i) { return S[Y + i]; }, k, [&](int i, double v) { S[F + i] = v; });
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[35 + i] = S[F + i];
+    }
+    solve(S, 35);
+    fun([&](int i) { return S[Y + i] + S[35 + i]; }, k, [&](int i, double v) { S[F + i] = v; });
+    const double c21 = -1.0156171083877703 / h;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[41 + i] = fma(c21, S[35 + i], S[F + i]);
+    }
+    solve(S, 41);
+    const double c31 = 4.0759956452537702 / h;
+    const double c32 = 9.20767942983308 / h;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      S[47 + i] = fma(c32, S[41 + i], fma(c31, S[35 + i], S[F + i]));
+    }
+    solve(S, 47);
+    double err_sq = 0.0;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      const double k0 = S[35 + i];
+      const double k1 = S[41 + i];
+      const double k2 = S[47 + i];
+      const double yi = S[Y + i];
+      const double ynew = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, yi + k0));
+      S[DY + i] = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, k0));
+      const double sc = fma(rtol_v(i), fmax(fabs(yi), fabs(ynew)), atol_v(i));
+      const double q = (fma(0.22354069897811571, k2, fma(-2.9079558716805471, k1, 0.5 * k0))) / sc;
+      err_sq = fma(q, q, err_sq);
+    }
+    return fmax(sqrt(err_sq / 7.0), 1.0e-10);
+  }
+
+  // Step-size factor from the error norm (integrate.j2:324-333).
+  __device__ __forceinline__ static double growth(double err) {
+    const double fac = 0.9 / cbrt(err);
+    return fmax(0.2, fmin(fac, 6.0));
+  }
+};
+
+}  // namespace mkpp_small_strato

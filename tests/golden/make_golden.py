@@ -1,0 +1,80 @@
+"""Regenerate the golden fixtures of tests/golden/ from the MKPP reference tree.
+
+Reads (never writes) the reference checkout given by --reference and stores
+small JSON fixtures, so the tests never need the reference at run time:
+
+* chapman_kokkos_10x60.json  final state of the reference's native Kokkos run
+  (reports/native-kokkos-5.1.1/final-mkpp-chapman.stdout.json) and its inputs
+  (benchmarks/solver_comparison/runners/mkpp/main.cpp:36-43);
+* chapman_scipy_reference.json  SciPy-Radau golden of the reference's
+  e2e test (tests/integration/e2e_validation/data/chapman_reference.json);
+* lu_tables_<mech>.json  the factorize_plan operation/product tables and the
+  solve_plan tables of the shipped generated code
+  (mkpp-generated/<mech>/supernodal_{factorize,solve}.hpp);
+* chapman_factorization_kat.json  the 13-slot known-answer test of
+  tests/integration/supernodal_factorization/test_factorization_parity.cpp.
+
+Usage: python tests/golden/make_golden.py --reference <MKPP checkout>
+"""
+import argparse
+import hashlib
+import json
+import re
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+
+def tables(text: str, name: str):
+    m = re.search(name + r"\[\] = \{(.*?)\};", text, re.S)
+    body = m.group(1)
+    rows = re.findall(r"\{([^{}]*)\}", body)
+    if rows:
+        return [[int(x) for x in r.replace(" ", "").split(",") if x] for r in rows]
+    return [int(x) for x in body.replace(" ", "").replace("\n", "").split(",") if x]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", required=True)
+    ref = Path(ap.parse_args().reference)
+    run = json.loads((ref / "reports/native-kokkos-5.1.1/final-mkpp-chapman.stdout.json").read_text())
+    vals = run["state"]["checkpoints"][0]["values"]
+    (HERE / "chapman_kokkos_10x60.json").write_text(json.dumps({
+        "source": "reports/native-kokkos-5.1.1/final-mkpp-chapman.stdout.json",
+        "tolerances": {"atol": 1e-3, "rtol": 1e-6},
+        "dt": 60.0, "steps": 10, "jvals": [1e-12, 1e-4],
+        "initial": {"O": 2.5e9, "O2": 5.1e18, "O3": 8.0e11, "M": 2.46e19},
+        "final": vals, "elapsed_ms": run["timing"]["elapsed_ms"], "cell_steps": run["timing"]["cell_steps"],
+    }, indent=1))
+    sci = json.loads((ref / "tests/integration/e2e_validation/data/chapman_reference.json").read_text())
+    keep = {k: sci[k] for k in ("species", "initial_conditions", "jvals", "time_span", "scipy_config", "expected_final")}
+    keep["source"] = "tests/integration/e2e_validation/data/chapman_reference.json"
+    keep["gate"] = {"rtol": 1e-4, "atol": 1.0, "source": "tests/integration/e2e_validation/test_scipy_validation.cpp:246-247"}
+    (HERE / "chapman_scipy_reference.json").write_text(json.dumps(keep, indent=1))
+    for mech in ("chapman", "small_strato", "saprc99", "ts1"):
+        fac = (ref / f"mkpp-generated/{mech}/supernodal_factorize.hpp").read_text()
+        sol = (ref / f"mkpp-generated/{mech}/supernodal_solve.hpp").read_text()
+        out = {
+            "source": f"mkpp-generated/{mech}/supernodal_factorize.hpp, supernodal_solve.hpp",
+            "operations": tables(fac, "operations"), "products": tables(fac, "products"),
+            "lower_offsets": tables(sol, "lower_offsets"), "upper_offsets": tables(sol, "upper_offsets"),
+            "diagonal": tables(sol, "diagonal"), "lower": tables(sol, "lower"), "upper": tables(sol, "upper"),
+        }
+        if mech == "ts1":
+            # Large: keep counts and a digest of the canonical tables only.
+            canon = json.dumps({k: v for k, v in out.items() if k != "source"}, separators=(",", ":"), sort_keys=True)
+            out = {"source": out["source"], "n_operations": len(out["operations"]), "n_products": len(out["products"]),
+                   "sha256": hashlib.sha256(canon.encode()).hexdigest()}
+        (HERE / f"lu_tables_{mech}.json").write_text(json.dumps(out, separators=(",", ":")))
+    kat = (ref / "tests/integration/supernodal_factorization/test_factorization_parity.cpp").read_text()
+    w = [float(x) for x in re.search(r"COMPACT_SIZE> w\{(.*?)\};", kat, re.S).group(1).replace("\n", "").split(",")]
+    dense = [float(x) for x in re.search(r"dense_logical_matrix\{(.*?)\};", kat, re.S).group(1).replace("\n", "").split(",")]
+    (HERE / "chapman_factorization_kat.json").write_text(json.dumps({
+        "source": "tests/integration/supernodal_factorization/test_factorization_parity.cpp",
+        "w": w, "rhs": [1.0, 2.0, 3.0, 4.0], "dense_logical": dense, "residual_tol": 1e-12}, indent=1))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

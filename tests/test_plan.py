@@ -1,0 +1,77 @@
+"""Structure of the exported plans against the reference's shipped generated tables."""
+import hashlib
+import json
+from pathlib import Path
+
+import pytest
+
+from mkpp_gb300.emitter import cuda_emitter
+from mkpp_gb300.emitter.plan import jacobian_pattern, load, load_raw
+
+GOLD = Path(__file__).resolve().parent / "golden"
+MECHS = ["chapman", "small_strato", "saprc99", "ts1"]
+
+
+def _tables(raw):
+    comp = raw["compact"]
+    lower = [list(e) for e in comp["lower"]]
+    upper = [list(e) for e in comp["upper"]]
+    return {
+        "operations": comp["operations"], "products": comp["products"],
+        "lower_offsets": comp["lower_offsets"], "upper_offsets": comp["upper_offsets"],
+        "diagonal": comp["diagonals"], "lower": lower, "upper": upper,
+    }
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_lu_schedule_matches_shipped_generated_code(mech):
+    """The exported Doolittle schedule is the one in mkpp-generated/<mech>/supernodal_*.hpp."""
+    gold = json.loads((GOLD / f"lu_tables_{mech}.json").read_text())
+    mine = _tables(load_raw(mech))
+    if "sha256" in gold:
+        canon = json.dumps(mine, separators=(",", ":"), sort_keys=True)
+        assert len(mine["operations"]) == gold["n_operations"]
+        assert len(mine["products"]) == gold["n_products"]
+        assert hashlib.sha256(canon.encode()).hexdigest() == gold["sha256"]
+    else:
+        for key in mine:
+            assert mine[key] == gold[key], key
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_reduced_plan_invariants(mech):
+    p = load(mech)
+    assert p.n_var + len(p.fixed_phys) == p.n_species
+    # mass-action Jacobian pattern == reference W off-diagonal pattern on variable species
+    offdiag = {loc for loc in p.w_slots if loc[0] != loc[1]}
+    pat = {x for x in jacobian_pattern(p) if x[0] != x[1]}
+    assert pat == offdiag
+    # every W slot is an LU slot; diagonals present; products reference earlier outputs only
+    assert set(p.w_slots) <= set(p.lu_slots)
+    written = set()
+    for out, w, b, e, dg in p.ops:
+        for q in range(b, e):
+            a, c = p.products[q]
+            assert a in written and c in written
+        if dg >= 0:
+            assert dg in written
+        written.add(out)
+    assert written == set(range(len(p.lu_slots)))
+
+
+@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99"])
+def test_generated_header_is_current(mech):
+    plan = load(mech)
+    text = cuda_emitter.emit_mechanism(plan)
+    path = cuda_emitter.GEN_DIR / f"{mech}.cuh"
+    assert path.read_text() == text, "regenerate with python -m mkpp_gb300.emitter.cuda_emitter"
+
+
+def test_tableaux_match_reference_coefficients():
+    """ROS-3 coefficients as in src/mkpp/rosenbrock.py:40-51 and chapman.hpp:190-191."""
+    tab = load_raw("chapman")["tableau"]
+    assert tab["name"] == "ROS-3" and tab["stages"] == 3
+    assert tab["Gamma"][0] == 0.435866521508459
+    assert tab["C"] == [-1.0156171083877703, 4.07599564525377, 9.20767942983308]
+    assert tab["M"] == [1.0, 6.1697947043828245, -0.42772256543218573]
+    assert tab["NewF"] == [True, True, False]
