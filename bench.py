@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--max-attempts", type=int, default=100000)
+    ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous host step)")
     return ap.parse_args()
 
 
@@ -250,18 +251,26 @@ def main():
         if rc != MKPP_SUCCESS:
             raise RuntimeError(f"{what} failed: {rc}")
 
+    order = torch.arange(n, dtype=torch.int32, device=dev)
+
     def one_run(mode=1, events=None):
         conc.copy_(conc0)
+        acc.zero_()
+        rej.zero_()
+        order.copy_(torch.arange(n, dtype=torch.int32, device=dev))
         for s in range(hs):
             check(lib.mkpp_gpu_rate_constants(C.c_size_t(n), p(conc), p(temp), p(rho), p(rh), None, p(params[s]),
                                               C.c_size_t(NP), p(ktab), p(status), sp), "rate constants")
             if events is not None:
                 events[s][0].record(stream)
             check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab), 1, C.c_double(w.dt), C.c_double(seed),
-                                           args.max_attempts, mode, p(status), p(acc[s]), p(rej[s]), p(ws),
-                                           C.c_size_t(ws.numel()), sp), "integrate")
+                                           args.max_attempts, mode, p(order) if args.order else None, p(status),
+                                           p(acc[s]), p(rej[s]), p(ws), C.c_size_t(ws.numel()), sp), "integrate")
             if events is not None:
                 events[s][1].record(stream)
+            if args.order and s + 1 < hs:
+                # Next host step hands out the cells that needed most attempts first.
+                order.copy_(torch.argsort(acc[s] + rej[s], descending=True).to(torch.int32))
 
     # Warm-up runs, eager, with events around every integrate launch.
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(hs)]
@@ -326,6 +335,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
         "gpu_launches": args.steps * hs * 2,
+        "launch": {"min_blocks": os.environ.get("MKPP_MIN_BLOCKS", "2"),
+                   "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"), "cost_order": bool(args.order)},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
                  "failed_cells": int((st_h != 0).sum())},

@@ -118,13 +118,15 @@ int mkpp_gpu_rate_constants(size_t num_cells, const double* conc, const double* 
 
 /* Integrate every cell `steps` times over dt seconds from precomputed rate
  * constants.  mode 0 = one thread per cell (plain), 1 = persistent work queue.
+ * cell_order (mode 1, may be NULL): a permutation of the cells giving the
+ * order in which the queue hands them out, e.g. most expensive first.
  * workspace: at least mkpp_gpu_workspace_bytes(num_cells) bytes of device
  * memory (queue counter and per-block scratch).  Cells whose status is non-zero on entry
  * are skipped.  Asynchronous on `stream`. */
 int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps,
-                         double dt, double seed, int max_attempts, int mode, int* status,
-                         int* accepted, int* rejected, void* workspace,
-                         size_t workspace_bytes, void* stream);
+                         double dt, double seed, int max_attempts, int mode,
+                         const int* cell_order, int* status, int* accepted, int* rejected,
+                         void* workspace, size_t workspace_bytes, void* stream);
 
 /* Same as mkpp_gpu_integrate_k, also recording every attempt's step size and
  * accept flag (log_h/log_acc[attempt * num_cells + cell], log_n[cell]) for

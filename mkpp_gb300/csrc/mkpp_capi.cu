@@ -86,26 +86,40 @@ int launch_grid(size_t cells, int block) { return (int)std::max<size_t>(1, (cell
 using StoreInfo = mkpp::StoreFor<Mech>;
 constexpr size_t kQueueBytes = 256;
 
-// Grid of the plain and persistent integrate kernels: SMs x resident blocks
-// per SM.  MKPP_BLOCKS_PER_SM caps the residency (fewer blocks keep the
-// per-block scratch tiles of large mechanisms closer to L2).
-int integrate_grid() {
-  static int grid = 0;
-  if (grid == 0) {
-    int dev = 0, sms = 0, per_sm = 0, per_sm_plain = 0;
+// Launch configuration of the integrate kernels: the register budget variant
+// (MKPP_MIN_BLOCKS = 1 or 2, see solver.cuh) and the grid, SMs x resident
+// blocks per SM.  MKPP_BLOCKS_PER_SM caps the residency (fewer blocks keep
+// the per-block scratch tiles of large mechanisms closer to L2).
+struct LaunchConfig {
+  int minb = 2;
+  int grid = 0;
+};
+
+template <int MINB>
+int resident_blocks() {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mkpp::integrate_persistent_kernel<Mech, MINB>, mkpp::kBlock, 0);
+  return std::max(1, per_sm);
+}
+
+const LaunchConfig& launch_config() {
+  static LaunchConfig cfg;
+  if (cfg.grid == 0) {
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mkpp::integrate_persistent_kernel<Mech>, mkpp::kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_plain, mkpp::integrate_plain_kernel<Mech>, mkpp::kBlock, 0);
-    per_sm = std::max(1, std::min(per_sm, per_sm_plain));
+    if (const char* env = std::getenv("MKPP_MIN_BLOCKS")) cfg.minb = std::atoi(env) == 4 ? 4 : 2;
+    int per_sm = cfg.minb == 4 ? resident_blocks<4>() : resident_blocks<2>();
     if (const char* env = std::getenv("MKPP_BLOCKS_PER_SM")) {
       const int cap = std::atoi(env);
       if (cap > 0) per_sm = std::min(per_sm, cap);
     }
-    grid = std::max(1, sms) * per_sm;
+    cfg.grid = std::max(1, sms) * per_sm;
   }
-  return grid;
+  return cfg;
 }
+
+int integrate_grid() { return launch_config().grid; }
 
 size_t workspace_bytes() { return kQueueBytes + (size_t)integrate_grid() * StoreInfo::block_bytes; }
 
@@ -132,11 +146,16 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   unsigned char* ws = (unsigned char*)workspace;
   a.queue = (unsigned int*)ws;
   double* scratch = StoreInfo::block_bytes ? (double*)(ws + kQueueBytes) : nullptr;
+  const LaunchConfig& cfg = launch_config();
   if (mode == 1) {
     if (cudaMemsetAsync(a.queue, 0, sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
-    mkpp::integrate_persistent_kernel<Mech><<<integrate_grid(), mkpp::kBlock, 0, stream>>>(a, scratch);
+    if (cfg.minb == 4)
+      mkpp::integrate_persistent_kernel<Mech, 4><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+    else
+      mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
   } else {
-    mkpp::integrate_plain_kernel<Mech><<<integrate_grid(), mkpp::kBlock, 0, stream>>>(a, scratch);
+    // The plain form runs with the same grid and the 255-register variant.
+    mkpp::integrate_plain_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
   }
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
@@ -600,13 +619,14 @@ static int check_integrate_args(size_t num_cells, const double* conc, const doub
 }
 
 int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps, double dt, double seed,
-                         int max_attempts, int mode, int* status, int* accepted, int* rejected, void* workspace,
-                         size_t workspace_bytes_, void* stream) {
+                         int max_attempts, int mode, const int* cell_order, int* status, int* accepted,
+                         int* rejected, void* workspace, size_t workspace_bytes_, void* stream) {
   const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
   if (rc != MKPP_SUCCESS) return rc;
   if (mode != 0 && mode != 1) return MKPP_ERROR_INVALID_ARGUMENT;
-  return launch_integrate(make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected),
-                          mode, workspace, (cudaStream_t)stream);
+  mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
+  a.order = cell_order;
+  return launch_integrate(a, mode, workspace, (cudaStream_t)stream);
 }
 
 int mkpp_gpu_integrate_logged(size_t num_cells, double* conc, const double* ktab, int steps, double dt, double seed,

@@ -33,6 +33,7 @@ struct LaunchArgs {
   int* n_accept;             // [ncells] or null (accumulated over steps)
   int* n_reject;             // [ncells] or null
   unsigned int* queue;       // persistent kernel work counter (zeroed before launch)
+  const int* order;          // persistent kernel: queue position -> cell, or null (identity)
   // Optional per-attempt log for step-sequence replay in the CPU oracle:
   // entry a of cell c at [a * ncells + c]; log_n[c] = attempts recorded.
   double* log_h;
@@ -235,13 +236,16 @@ __device__ __forceinline__ int integrate_cell(SA& S, const KA& k, const LaunchAr
   return status;
 }
 
+// MINB is the launch-bounds minimum of resident blocks per SM: 2 lets each
+// thread use up to 255 registers (2 blocks of 128 fit), 4 caps it at 128 so
+// that 4 blocks can be resident, trading spills for latency hiding.
 // ---------------------------------------------------------------------------
 // Plain form: a fixed grid, thread t integrates cells t, t + T, t + 2T, ...
 // (T = grid threads) one after the other.  A warp runs until its slowest
 // lane is done, so lanes with easy cells idle while stiff ones finish.
 // ---------------------------------------------------------------------------
-template <class Mech>
-__global__ void __launch_bounds__(kBlock, 1) integrate_plain_kernel(LaunchArgs a, double* scratch) {
+template <class Mech, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) integrate_plain_kernel(LaunchArgs a, double* scratch) {
   using Store = typename StoreFor<Mech>::type;
   Store S = make_store<Mech>(scratch, (Store*)nullptr);
   const size_t n = (size_t)a.ncells;
@@ -265,8 +269,8 @@ __global__ void __launch_bounds__(kBlock, 1) integrate_plain_kernel(LaunchArgs a
 // so a warp's lanes stay busy even when cells need very different numbers
 // of attempts.  All lanes run the same attempt code on different cells.
 // ---------------------------------------------------------------------------
-template <class Mech>
-__global__ void __launch_bounds__(kBlock, 1) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
+template <class Mech, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
   using Store = typename StoreFor<Mech>::type;
   Store S = make_store<Mech>(scratch, (Store*)nullptr);
   const size_t n = (size_t)a.ncells;
@@ -287,6 +291,7 @@ __global__ void __launch_bounds__(kBlock, 1) integrate_persistent_kernel(LaunchA
       base = __shfl_sync(0xffffffffu, base, leader);
       if (need) {
         cell = (long long)base + __popc(want & lt_mask);
+        if (cell < (long long)n && a.order) cell = a.order[cell];
         if (cell < (long long)n) {
           status = a.status ? a.status[cell] : CELL_SUCCESS;
           flagged = status != CELL_SUCCESS;

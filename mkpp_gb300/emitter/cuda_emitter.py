@@ -96,6 +96,34 @@ def _sum_expr(init: str | None, terms: list[tuple[float, str]]) -> str:
     return _accumulate("@", init, terms)[4:-1]
 
 
+ILP_GROUP = 8
+
+
+def _interleave(c, plan, ops, operands, scale):
+    """Emit the dot products of independent LU ops in interleaved rounds.
+
+    ops are (out, w, begin, end, diag) with disjoint outputs that read only
+    values finished earlier.  Groups of ILP_GROUP ops advance one product per
+    round, which keeps each op's subtraction order (and so its rounding)
+    exactly that of the sequential schedule.
+    """
+    for g in range(0, len(ops), ILP_GROUP):
+        grp = ops[g:g + ILP_GROUP]
+        for out, w, b, e, dg in grp:
+            c(f"      double v{out} = {'S[%d]' % out if w >= 0 else '0.0'};")
+        longest = max(e - b for _, _, b, e, _ in grp)
+        for t in range(longest):
+            for out, w, b, e, dg in grp:
+                if b + t < e:
+                    x, y = operands(b + t)
+                    c(f"      v{out} = fma(-{x}, {y}, v{out});")
+        for out, w, b, e, dg in grp:
+            if scale:
+                c(f"      S[{out}] = v{out} * {scale};")
+            elif not (w >= 0 and e == b):
+                c(f"      S[{out}] = v{out};")
+
+
 def emit_mechanism(plan: ReducedPlan) -> str:
     raw = plan.raw
     name = plan.name
@@ -314,29 +342,27 @@ def emit_mechanism(plan: ReducedPlan) -> str:
         lslots = sorted({plan.products[q][0] for o in upart for q in range(o[2], o[3])})
         for sl in lslots:
             c(f"      const double a{sl} = S[{sl}];")
-        rd = None
-        for out, w, b, e, dg in upart:
+        # The diagonal U_ii comes first in the reference order; it only
+        # depends on earlier rows, so it can be finished (and inverted) before
+        # the rest of the row.  The remaining independent dot products of the
+        # row advance together, one product per op per round, so the FP64 pipe
+        # sees several independent chains; each op keeps its own product order.
+        diag_op = [o for o in upart if o[0] in diag_slots]
+        rest_u = [o for o in upart if o[0] not in diag_slots]
+        for out, w, b, e, dg in diag_op:
             expr = f"S[{out}]" if w >= 0 else "0.0"
             for q in range(b, e):
                 l_, u_ = plan.products[q]
                 expr = f"fma(-a{l_}, S[{u_}], {expr})"
-            if out in diag_slots:
-                c(f"      const double u{out} = {expr};")
-                c(f"      ok = ok && (u{out} != 0.0);")
-                c(f"      const double rd = 1.0 / u{out};")
-                c(f"      S[{out}] = rd;")
-                rd = "rd"
-            elif expr != f"S[{out}]":
-                c(f"      S[{out}] = {expr};")
+            c(f"      const double u{out} = {expr};")
+            c(f"      ok = ok && (u{out} != 0.0);")
+            c(f"      const double rd = 1.0 / u{out};")
+            c(f"      S[{out}] = rd;")
+        _interleave(c, plan, rest_u, lambda q: (f"a{plan.products[q][0]}", f"S[{plan.products[q][1]}]"), None)
         uslots = sorted({plan.products[q][1] for o in lpart for q in range(o[2], o[3])})
         for sl in uslots:
             c(f"      const double b{sl} = S[{sl}];")
-        for out, w, b, e, dg in lpart:
-            expr = f"S[{out}]" if w >= 0 else "0.0"
-            for q in range(b, e):
-                l_, u_ = plan.products[q]
-                expr = f"fma(-S[{l_}], b{u_}, {expr})"
-            c(f"      S[{out}] = ({expr}) * rd;")
+        _interleave(c, plan, lpart, lambda q: (f"S[{plan.products[q][0]}]", f"b{plan.products[q][1]}"), "rd")
         c("    }")
     c("    return ok;")
     c("  }")

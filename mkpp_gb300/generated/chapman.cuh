@@ -137,8 +137,12 @@ struct Mech {
       ok = ok && (u0 != 0.0);
       const double rd = 1.0 / u0;
       S[0] = rd;
-      S[3] = (S[3]) * rd;
-      S[6] = (S[6]) * rd;
+      double v1 = S[1];
+      double v2 = S[2];
+      double v3 = S[3];
+      double v6 = S[6];
+      S[3] = v3 * rd;
+      S[6] = v6 * rd;
     }
     {  // pivot row 1
       const double a3 = S[3];
@@ -146,9 +150,13 @@ struct Mech {
       ok = ok && (u4 != 0.0);
       const double rd = 1.0 / u4;
       S[4] = rd;
-      S[5] = fma(-a3, S[2], S[5]);
+      double v5 = S[5];
+      v5 = fma(-a3, S[2], v5);
+      S[5] = v5;
       const double b1 = S[1];
-      S[7] = (fma(-S[6], b1, S[7])) * rd;
+      double v7 = S[7];
+      v7 = fma(-S[6], b1, v7);
+      S[7] = v7 * rd;
     }
     {  // pivot row 2
       const double a6 = S[6];

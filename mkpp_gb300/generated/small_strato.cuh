@@ -200,9 +200,13 @@ struct Mech {
       ok = ok && (u0 != 0.0);
       const double rd = 1.0 / u0;
       S[0] = rd;
-      S[2] = (S[2]) * rd;
-      S[7] = (S[7]) * rd;
-      S[13] = (S[13]) * rd;
+      double v1 = S[1];
+      double v2 = S[2];
+      double v7 = S[7];
+      double v13 = S[13];
+      S[2] = v2 * rd;
+      S[7] = v7 * rd;
+      S[13] = v13 * rd;
     }
     {  // pivot row 1
       const double a2 = S[2];
@@ -210,11 +214,19 @@ struct Mech {
       ok = ok && (u3 != 0.0);
       const double rd = 1.0 / u3;
       S[3] = rd;
-      S[5] = fma(-a2, S[1], S[5]);
-      S[8] = (S[8]) * rd;
-      S[14] = (S[14]) * rd;
-      S[19] = (S[19]) * rd;
-      S[24] = (S[24]) * rd;
+      double v4 = S[4];
+      double v5 = S[5];
+      double v6 = S[6];
+      v5 = fma(-a2, S[1], v5);
+      S[5] = v5;
+      double v8 = S[8];
+      double v14 = S[14];
+      double v19 = S[19];
+      double v24 = S[24];
+      S[8] = v8 * rd;
+      S[14] = v14 * rd;
+      S[19] = v19 * rd;
+      S[24] = v24 * rd;
     }
     {  // pivot row 2
       const double a7 = S[7];
@@ -223,12 +235,24 @@ struct Mech {
       ok = ok && (u9 != 0.0);
       const double rd = 1.0 / u9;
       S[9] = rd;
-      S[10] = fma(-a8, S[5], fma(-a7, S[1], S[10]));
-      S[12] = fma(-a8, S[6], S[12]);
+      double v10 = S[10];
+      double v11 = S[11];
+      double v12 = S[12];
+      v10 = fma(-a7, S[1], v10);
+      v12 = fma(-a8, S[6], v12);
+      v10 = fma(-a8, S[5], v10);
+      S[10] = v10;
+      S[12] = v12;
       const double b4 = S[4];
-      S[15] = (fma(-S[14], b4, S[15])) * rd;
-      S[20] = (fma(-S[19], b4, 0.0)) * rd;
-      S[25] = (fma(-S[24], b4, 0.0)) * rd;
+      double v15 = S[15];
+      double v20 = 0.0;
+      double v25 = 0.0;
+      v15 = fma(-S[14], b4, v15);
+      v20 = fma(-S[19], b4, v20);
+      v25 = fma(-S[24], b4, v25);
+      S[15] = v15 * rd;
+      S[20] = v20 * rd;
+      S[25] = v25 * rd;
     }
     {  // pivot row 3
       const double a13 = S[13];
@@ -238,12 +262,23 @@ struct Mech {
       ok = ok && (u16 != 0.0);
       const double rd = 1.0 / u16;
       S[16] = rd;
-      S[17] = fma(-a15, S[11], S[17]);
-      S[18] = fma(-a15, S[12], fma(-a14, S[6], 0.0));
+      double v17 = S[17];
+      double v18 = 0.0;
+      v17 = fma(-a15, S[11], v17);
+      v18 = fma(-a14, S[6], v18);
+      v18 = fma(-a15, S[12], v18);
+      S[17] = v17;
+      S[18] = v18;
       const double b5 = S[5];
       const double b10 = S[10];
-      S[21] = (fma(-S[20], b10, fma(-S[19], b5, S[21]))) * rd;
-      S[26] = (fma(-S[25], b10, fma(-S[24], b5, S[26]))) * rd;
+      double v21 = S[21];
+      double v26 = S[26];
+      v21 = fma(-S[19], b5, v21);
+      v26 = fma(-S[24], b5, v26);
+      v21 = fma(-S[20], b10, v21);
+      v26 = fma(-S[25], b10, v26);
+      S[21] = v21 * rd;
+      S[26] = v26 * rd;
     }
     {  // pivot row 4
       const double a19 = S[19];
@@ -253,10 +288,17 @@ struct Mech {
       ok = ok && (u22 != 0.0);
       const double rd = 1.0 / u22;
       S[22] = rd;
-      S[23] = fma(-a21, S[18], fma(-a20, S[12], fma(-a19, S[6], S[23])));
+      double v23 = S[23];
+      v23 = fma(-a19, S[6], v23);
+      v23 = fma(-a20, S[12], v23);
+      v23 = fma(-a21, S[18], v23);
+      S[23] = v23;
       const double b11 = S[11];
       const double b17 = S[17];
-      S[27] = (fma(-S[26], b17, fma(-S[25], b11, S[27]))) * rd;
+      double v27 = S[27];
+      v27 = fma(-S[25], b11, v27);
+      v27 = fma(-S[26], b17, v27);
+      S[27] = v27 * rd;
     }
     {  // pivot row 5
       const double a24 = S[24];
