@@ -200,7 +200,9 @@ def workload_config(w, hs):
     return {"workload": f"{w.mechanism}: {w.ncells} cells x {hs} host steps of {w.dt:g} s, ROS-3, "
                         f"rtol {raw['rtol'][0]:g}, atol {raw['atol'][0]:g}",
             "mechanism": w.mechanism, "cells_per_gpu": w.ncells, "host_steps": hs, "dt_s": w.dt,
-            "tableau": raw["tableau"]["name"], "form": "persistent work-queue kernel, 24 host steps in one CUDA graph",
+            "tableau": raw["tableau"]["name"],
+            "form": "CUDA graph per window: rate constants of every host step, then one persistent work-queue "
+                    "launch carrying each cell through all host steps (cells ordered by the previous window's cost)",
             "l2": "inputs larger than L2 (concentrations + rate-constant table > 129 MB)"}
 
 
@@ -237,10 +239,12 @@ def main():
     rho = torch.from_numpy(w.rho).to(dev)
     rh = torch.from_numpy(w.rh).to(dev)
     params = torch.from_numpy(np.stack([w.param_at(s) for s in range(hs)])).to(dev)
-    ktab = torch.empty((NR, n), dtype=f64, device=dev)
+    # Rate constants of every host step of the window: [hs][NR][n].
+    ktab = torch.empty((hs, NR, n), dtype=f64, device=dev)
     status = torch.zeros(n, dtype=torch.int32, device=dev)
-    acc = torch.zeros((hs, n), dtype=torch.int32, device=dev)
-    rej = torch.zeros((hs, n), dtype=torch.int32, device=dev)
+    acc = torch.zeros(n, dtype=torch.int32, device=dev)
+    rej = torch.zeros(n, dtype=torch.int32, device=dev)
+    order = torch.arange(n, dtype=torch.int32, device=dev)
     ws_bytes = int(lib.mkpp_gpu_workspace_bytes(C.c_size_t(n)))
     ws = torch.zeros(max(ws_bytes, 256), dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
@@ -251,40 +255,40 @@ def main():
         if rc != MKPP_SUCCESS:
             raise RuntimeError(f"{what} failed: {rc}")
 
-    order = torch.arange(n, dtype=torch.int32, device=dev)
-
-    def one_run(mode=1, events=None):
-        conc.copy_(conc0)
-        acc.zero_()
-        rej.zero_()
-        order.copy_(torch.arange(n, dtype=torch.int32, device=dev))
+    def rates():
         for s in range(hs):
             check(lib.mkpp_gpu_rate_constants(C.c_size_t(n), p(conc), p(temp), p(rho), p(rh), None, p(params[s]),
-                                              C.c_size_t(NP), p(ktab), p(status), sp), "rate constants")
-            if events is not None:
-                events[s][0].record(stream)
-            check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab), 1, C.c_double(w.dt), C.c_double(seed),
-                                           args.max_attempts, mode, p(order) if args.order else None, p(status),
-                                           p(acc[s]), p(rej[s]), p(ws), C.c_size_t(ws.numel()), sp), "integrate")
-            if events is not None:
-                events[s][1].record(stream)
-            if args.order and s + 1 < hs:
-                # Next host step hands out the cells that needed most attempts first.
-                order.copy_(torch.argsort(acc[s] + rej[s], descending=True).to(torch.int32))
+                                              C.c_size_t(NP), p(ktab[s]), p(status) if s == 0 else None, sp),
+                  "rate constants")
 
-    # Warm-up runs, eager, with events around every integrate launch.
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(hs)]
+    def window(events=None):
+        """The persistent form: all host steps of every cell in one launch,
+        cells handed out most expensive first (cost of the previous window)."""
+        conc.copy_(conc0)
+        rates()
+        if events is not None:
+            events[0].record(stream)
+        check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab), C.c_size_t(NR * n), hs, C.c_double(w.dt),
+                                       C.c_double(seed), args.max_attempts, 1, p(order) if args.order else None,
+                                       p(status), p(acc), p(rej), p(ws), C.c_size_t(ws.numel()), sp), "integrate")
+        if events is not None:
+            events[1].record(stream)
+        if args.order:
+            order.copy_(torch.argsort(acc + rej, descending=True).to(torch.int32))
+
+    # Warm-up windows, eager, with events around the integrate launch.
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     kernel_ms = []
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
-            one_run(1, ev)
+            window(ev)
             stream.synchronize()
-            kernel_ms.append([a.elapsed_time(b) for a, b in ev])
-    # Capture the 24 host steps as one graph.
+            kernel_ms.append(ev[0].elapsed_time(ev[1]))
+    # Capture the window (hs rate-constant launches + 1 integrate launch).
     g = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
         with torch.cuda.graph(g, stream=stream):
-            one_run(1)
+            window()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -301,16 +305,14 @@ def main():
     cell_solves = n * hs * world
     value = cell_solves / (el_ms * 1e-3)
 
-    # Work counters of the (deterministic) run just timed.
-    acc_h, rej_h = acc.cpu().numpy(), rej.cpu().numpy()
+    # Work counters of the (deterministic) window just timed.
+    att = (acc + rej).cpu().numpy().astype(np.int64)
     st_h = status.cpu().numpy()
-    attempts = int(acc_h.sum()) + int(rej_h.sum())
+    attempts = int(att.sum())
     fpa = flops_per_attempt(plan)
     flops_run = attempts * fpa["total"]
-    # Dominant kernel: the integrate launches; average per launch over the last warm-up run.
-    per_launch_ms = statistics.mean(kernel_ms[-1]) if kernel_ms else float("nan")
-    kernel_total_ms = sum(kernel_ms[-1]) if kernel_ms else float("nan")
-    achieved = flops_run / (kernel_total_ms * 1e-3) / 1e12 if kernel_ms else None
+    kernel_avg_ms = statistics.mean(kernel_ms[1:] or kernel_ms) if kernel_ms else float("nan")
+    achieved = flops_run / (kernel_avg_ms * 1e-3) / 1e12 if kernel_ms else None
 
     # Live FP64 FMA peak (DFMA probe on this GPU).
     probe = C.CDLL(str(ROOT / "mkpp_gb300" / "lib" / "libmkpp_probe.so"))
@@ -334,34 +336,41 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
-        "gpu_launches": args.steps * hs * 2,
+        "gpu_launches": args.steps * (hs + 1),
         "launch": {"min_blocks": os.environ.get("MKPP_MIN_BLOCKS", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"), "cost_order": bool(args.order)},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
-                 "failed_cells": int((st_h != 0).sum())},
+                 "attempts_per_cell_window_pct": {q: float(np.percentile(att, q)) for q in (50, 90, 99, 100)},
+                 "cell_status_counts": np.bincount(st_h, minlength=5).tolist()},
         "roofline": {
             "bound": "fp64", "achieved": achieved, "peak": best, "unit": "TFLOP/s",
             "frac": (achieved / best) if achieved and best else None,
             "peak_source": "measured live: DFMA probe (csrc/probe.cu) on this GPU",
-            "kernel": "integrate_persistent_kernel", "launch_ms_avg": per_launch_ms,
-            "algorithmic_flops_per_launch": flops_run / hs,
+            "kernel": "integrate_persistent_kernel", "launch_ms_avg": kernel_avg_ms,
+            "algorithmic_flops_per_launch": flops_run,
             "traffic": None,
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
         },
     }
 
     if rank == 0 and not args.no_plain:
-        # Plain form: one thread per cell, per-launch, no graph, same inputs.
+        # Plain form: one launch per host step, one thread per cell, no queue.
         pe = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         with torch.cuda.stream(stream):
             pe[0].record(stream)
-            one_run(0)
+            conc.copy_(conc0)
+            rates()
+            for s in range(hs):
+                check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab[s]), C.c_size_t(0), 1,
+                                               C.c_double(w.dt), C.c_double(seed), args.max_attempts, 0, None,
+                                               p(status), p(acc), p(rej), p(ws), C.c_size_t(ws.numel()), sp),
+                      "integrate plain")
             pe[1].record(stream)
             stream.synchronize()
         pm = pe[0].elapsed_time(pe[1])
         result["plain_form"] = {"value": n * hs / (pm * 1e-3), "unit": UNIT, "ms_per_step": pm,
-                                "form": "one thread per cell, 48 eager launches"}
+                                "form": f"one thread per cell, one launch per host step ({2 * hs} eager launches)"}
 
     if not args.no_e2e:
         # End to end through the reference-facing host C ABI with pinned host buffers.

@@ -116,15 +116,22 @@ int mkpp_gpu_rate_constants(size_t num_cells, const double* conc, const double* 
                             const double* param, size_t num_params, double* ktab,
                             int* status, void* stream);
 
-/* Integrate every cell `steps` times over dt seconds from precomputed rate
- * constants.  mode 0 = one thread per cell (plain), 1 = persistent work queue.
+/* Integrate every cell over `steps` consecutive host steps of dt seconds
+ * from precomputed rate constants: host step s reads the rate table at
+ * ktab + s * k_step_stride (k_step_stride = 0: the same rate constants for
+ * every step, like the reference's repeated integrate() calls; otherwise at
+ * least num_cells * reactions).  A cell runs through all its host steps
+ * before its thread takes the next cell.
+ * mode 0 = one thread per cell (plain), 1 = persistent work queue.
  * cell_order (mode 1, may be NULL): a permutation of the cells giving the
  * order in which the queue hands them out, e.g. most expensive first.
  * workspace: at least mkpp_gpu_workspace_bytes(num_cells) bytes of device
- * memory (queue counter and per-block scratch).  Cells whose status is non-zero on entry
- * are skipped.  Asynchronous on `stream`. */
-int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps,
-                         double dt, double seed, int max_attempts, int mode,
+ * memory (queue counter and per-block scratch).  Cells whose status is
+ * non-zero on entry are skipped; on exit status holds each cell's outcome
+ * (MKPP_CELL_*).  Asynchronous on `stream`. */
+int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab,
+                         size_t k_step_stride, int steps, double dt, double seed,
+                         int max_attempts, int mode,
                          const int* cell_order, int* status, int* accepted, int* rejected,
                          void* workspace, size_t workspace_bytes, void* stream);
 

@@ -74,7 +74,7 @@ SIGNATURES = [
     ("mkpp_mechanism_sizes", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("mkpp_gpu_workspace_bytes", _sz, [_sz]),
     ("mkpp_gpu_rate_constants", _i, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
-    ("mkpp_gpu_integrate_k", _i, [_sz, _vp, _vp, _i, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    ("mkpp_gpu_integrate_k", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_integrate_logged", _i, [_sz, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _sz,
                                        _vp]),
     ("mkpp_gpu_evaluate_rates", _i, [_sz, _vp, _vp, _vp, _vp]),
@@ -300,15 +300,15 @@ class DeviceSolver:
         return ktab, status
 
     def integrate_k(self, conc, ktab, dt, steps=1, seed=None, max_attempts=100000, mode="persistent",
-                    status=None, accepted=None, rejected=None, order=None):
+                    status=None, accepted=None, rejected=None, order=None, k_step_stride=0):
         torch = self.torch
         ns, n = conc.shape
         if seed is None:
             seed = self.default_seed
         ws = self.workspace(n)
         rc = self.lib.mkpp_gpu_integrate_k(
-            C.c_size_t(n), _ptr(conc), _ptr(ktab), C.c_int(steps), C.c_double(dt), C.c_double(seed),
-            C.c_int(max_attempts), C.c_int(MODES[mode]), _ptr(order), _ptr(status), _ptr(accepted), _ptr(rejected),
+            C.c_size_t(n), _ptr(conc), _ptr(ktab), C.c_size_t(k_step_stride), C.c_int(steps), C.c_double(dt),
+            C.c_double(seed), C.c_int(max_attempts), C.c_int(MODES[mode]), _ptr(order), _ptr(status), _ptr(accepted), _ptr(rejected),
             _ptr(ws), C.c_size_t(ws.numel()), self._stream())
         self._check(rc)
 

@@ -618,14 +618,16 @@ static int check_integrate_args(size_t num_cells, const double* conc, const doub
   return MKPP_SUCCESS;
 }
 
-int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, int steps, double dt, double seed,
-                         int max_attempts, int mode, const int* cell_order, int* status, int* accepted,
-                         int* rejected, void* workspace, size_t workspace_bytes_, void* stream) {
+int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, size_t k_step_stride, int steps,
+                         double dt, double seed, int max_attempts, int mode, const int* cell_order, int* status,
+                         int* accepted, int* rejected, void* workspace, size_t workspace_bytes_, void* stream) {
   const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
   if (rc != MKPP_SUCCESS) return rc;
   if (mode != 0 && mode != 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (k_step_stride != 0 && k_step_stride < num_cells * Mech::NR) return MKPP_ERROR_INVALID_ARGUMENT;
   mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
   a.order = cell_order;
+  a.k_step_stride = k_step_stride;
   return launch_integrate(a, mode, workspace, (cudaStream_t)stream);
 }
 

@@ -28,7 +28,9 @@ struct LaunchArgs {
   double seed;               // initial_step_seed
   int max_attempts;          // per integrate() call
   double* conc;              // [NS][ncells]
-  const double* ktab;        // [NR][ncells]
+  const double* ktab;        // [NR][ncells] (host step 0)
+  size_t k_step_stride;      // doubles between the rate tables of consecutive host
+                             // steps (0: the same rate constants for every step)
   int* status;               // [ncells] or null
   int* n_accept;             // [ncells] or null (accumulated over steps)
   int* n_reject;             // [ncells] or null
@@ -198,25 +200,38 @@ __device__ __forceinline__ void apply_increment(SA& S) {
   for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] += S[Mech::DY + i];
 }
 
+// Final status of a cell: non-finite state, attempt cap, zero pivot seen.
+// A zero pivot does not stop the cell: like the reference (which has no
+// singularity check) it runs on, and a non-finite result is reported as
+// CELL_ERR_NUMERICAL_FAILURE; a finite result after a zero pivot keeps
+// CELL_ERR_SINGULAR_MATRIX.
+template <class Mech, class SA>
+__device__ __forceinline__ int final_status(SA& S, bool capped, bool zero_pivot) {
+  if (!state_finite<Mech>(S)) return CELL_ERR_NUMERICAL_FAILURE;
+  if (capped) return CELL_ERR_CONVERGENCE_FAILURE;
+  return zero_pivot ? CELL_ERR_SINGULAR_MATRIX : CELL_SUCCESS;
+}
+
 // One cell, `steps` integrate() calls; the plain kernel's per-cell body.
-template <class Mech, class SA, class KA>
-__device__ __forceinline__ int integrate_cell(SA& S, const KA& k, const LaunchArgs& a, size_t c, int& nacc,
-                                              int& nrej) {
+template <class Mech, class SA>
+__device__ __forceinline__ int integrate_cell(SA& S, const LaunchArgs& a, size_t c, int& nacc, int& nrej) {
   const size_t n = (size_t)a.ncells;
-  int status = CELL_SUCCESS, logged = 0;
+  int logged = 0;
+  bool capped = false, zero_pivot = false;
   nacc = nrej = 0;
-  for (int step = 0; step < a.steps && status == CELL_SUCCESS; ++step) {
+  for (int step = 0; step < a.steps && !capped; ++step) {
+    const KTable k{a.ktab + (size_t)step * a.k_step_stride + c, n};
     Controller ctl;
     ctl.start(a.dt, a.seed);
     while (ctl.running()) {
       if (ctl.attempts >= a.max_attempts) {
-        status = CELL_ERR_CONVERGENCE_FAILURE;
+        capped = true;
         break;
       }
       const double h = ctl.next_h();
       int st = 0;
       const double err = Mech::attempt(S, k, h, st);
-      if (st) status = CELL_ERR_SINGULAR_MATRIX;
+      zero_pivot |= st != 0;
       const bool acc = ctl.update<Mech>(err);
       if (a.log_h && logged < a.log_cap) {
         a.log_h[(size_t)logged * n + c] = h;
@@ -232,8 +247,7 @@ __device__ __forceinline__ int integrate_cell(SA& S, const KA& k, const LaunchAr
     }
   }
   if (a.log_n) a.log_n[c] = logged;
-  if (status == CELL_SUCCESS && !state_finite<Mech>(S)) status = CELL_ERR_NUMERICAL_FAILURE;
-  return status;
+  return final_status<Mech>(S, capped, zero_pivot);
 }
 
 // MINB is the launch-bounds minimum of resident blocks per SM: 2 lets each
@@ -253,9 +267,8 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_plain_kernel(LaunchArg
   for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
     if (a.status && a.status[c] != CELL_SUCCESS) continue;
     load_state<Mech>(a.conc, c, n, S);
-    const KTable k{a.ktab + c, n};
     int nacc, nrej;
-    const int status = integrate_cell<Mech>(S, k, a, c, nacc, nrej);
+    const int status = integrate_cell<Mech>(S, a, c, nacc, nrej);
     store_state<Mech>(a.conc, c, n, S);
     if (a.status) a.status[c] = status;
     if (a.n_accept) a.n_accept[c] = nacc;
@@ -277,8 +290,9 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   long long cell = -1;       // -1: needs work; >= n: queue exhausted
-  int step = 0, status = CELL_SUCCESS, nacc = 0, nrej = 0;
+  int step = 0, nacc = 0, nrej = 0;
   bool flagged = false;      // cell rejected by the input checks: leave it untouched
+  bool capped = false, zero_pivot = false;
   Controller ctl;
   ctl.start(a.dt, a.seed);
   for (;;) {
@@ -293,11 +307,11 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         cell = (long long)base + __popc(want & lt_mask);
         if (cell < (long long)n && a.order) cell = a.order[cell];
         if (cell < (long long)n) {
-          status = a.status ? a.status[cell] : CELL_SUCCESS;
-          flagged = status != CELL_SUCCESS;
+          flagged = a.status && a.status[cell] != CELL_SUCCESS;
           step = 0;
           nacc = nrej = 0;
-          if (status == CELL_SUCCESS) load_state<Mech>(a.conc, (size_t)cell, n, S);
+          capped = zero_pivot = false;
+          if (!flagged) load_state<Mech>(a.conc, (size_t)cell, n, S);
           ctl.start(a.dt, a.seed);
         }
       }
@@ -305,17 +319,17 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
     const bool active = cell >= 0 && cell < (long long)n;
     if (__ballot_sync(0xffffffffu, active) == 0u) break;
     if (!active) continue;
-    bool done = status != CELL_SUCCESS;
+    bool done = flagged;
     if (!done) {
       if (ctl.attempts >= a.max_attempts) {
-        status = CELL_ERR_CONVERGENCE_FAILURE;
+        capped = true;
         done = true;
       } else {
-        const KTable k{a.ktab + cell, n};
+        const KTable k{a.ktab + (size_t)step * a.k_step_stride + cell, n};
         const double h = ctl.next_h();
         int st = 0;
         const double err = Mech::attempt(S, k, h, st);
-        if (st) status = CELL_ERR_SINGULAR_MATRIX;
+        zero_pivot |= st != 0;
         if (ctl.update<Mech>(err)) {
           apply_increment<Mech>(S);
           ++nacc;
@@ -323,18 +337,16 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           ++nrej;
         }
         if (!ctl.running()) {
-          if (++step < a.steps && status == CELL_SUCCESS) ctl.start(a.dt, a.seed);
+          if (++step < a.steps) ctl.start(a.dt, a.seed);
           else done = true;
         }
-        if (status != CELL_SUCCESS) done = true;
       }
     }
     if (done) {
       const size_t cc = (size_t)cell;
       if (!flagged) {
-        if (status == CELL_SUCCESS && !state_finite<Mech>(S)) status = CELL_ERR_NUMERICAL_FAILURE;
         store_state<Mech>(a.conc, cc, n, S);
-        if (a.status) a.status[cc] = status;
+        if (a.status) a.status[cc] = final_status<Mech>(S, capped, zero_pivot);
         if (a.n_accept) a.n_accept[cc] = nacc;
         if (a.n_reject) a.n_reject[cc] = nrej;
       }

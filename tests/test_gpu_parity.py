@@ -238,3 +238,26 @@ def test_c_abi_argument_errors(built_libs):
     with pytest.raises(MkppError):
         ctx.species_index("XX")
     assert ctx.photolysis_index("J_2") == 1
+
+
+def test_windowed_launch_equals_per_step_launches(built_libs):
+    """One persistent launch over 3 host steps (own rate table per step) ==
+    3 launches, one per host step."""
+    torch = _torch()
+    w, s, o = _setup("small_strato", 256)
+    n = w.ncells
+    params = [w.param * f for f in (1.0, 0.3, 0.0)]
+    ktabs = []
+    for prm in params:
+        k, _ = s.rate_constants(_dev(w.conc), param=_dev(prm))
+        ktabs.append(k)
+    kall = torch.stack(ktabs).contiguous()
+    a = _dev(w.conc)
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    s.integrate_k(a, kall, w.dt, steps=3, k_step_stride=kall[0].numel(), mode="persistent", status=st)
+    b = _dev(w.conc)
+    for k in ktabs:
+        s.integrate_k(b, k, w.dt, steps=1, mode="plain")
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    assert int(st.sum()) == 0
