@@ -337,7 +337,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
         "gpu_launches": args.steps * (hs + 1),
-        "launch": {"min_blocks": os.environ.get("MKPP_MIN_BLOCKS", "2"),
+        "launch": {"min_blocks": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"), "cost_order": bool(args.order)},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],

@@ -102,10 +102,19 @@ int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions
 
 /* ---- Device-pointer entry points (no reference counterpart) ----------- */
 
-/* Workspace bytes mkpp_gpu_integrate_k / _logged need: a queue counter plus
- * the per-block LU/stage scratch tiles of the integrate grid (sized to this
- * GPU, independent of num_cells).  The workspace must be 256-byte aligned. */
+/* Workspace bytes mkpp_gpu_integrate_k / _logged need for num_cells cells:
+ * work counters, the per-block LU/stage scratch tiles of the integrate grid
+ * and one parked-cell record per cell.  Depends on the launch tuning: query it
+ * after mkpp_set_launch_tuning.  The workspace must be 256-byte aligned. */
 size_t mkpp_gpu_workspace_bytes(size_t num_cells);
+
+/* Process-wide launch tuning of the integrate kernels (the autotuner's
+ * knobs): register_variant 2 (up to 255 registers per thread) or 4 (up to
+ * 128, more resident warps), 0 keeps the current one; blocks_per_sm caps the
+ * resident blocks per SM (0: as many as fit); defer_after: attempts within one
+ * host step after which the persistent kernel hands a cell to the
+ * warp-cooperative kernel (0: never, -1 keeps the current value). */
+int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after);
 
 /* Rate constants of every reaction into ktab[cell + num_cells * reaction].
  * temp/rho/rh/clw/param may be NULL (compile-time environment, 0.5, 0, zeros).

@@ -73,6 +73,7 @@ SIGNATURES = [
     ("mkpp_mechanism_name", _i, [_vp]),
     ("mkpp_mechanism_sizes", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("mkpp_gpu_workspace_bytes", _sz, [_sz]),
+    ("mkpp_set_launch_tuning", _i, [_i, _i, _i]),
     ("mkpp_gpu_rate_constants", _i, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     ("mkpp_gpu_integrate_k", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_integrate_logged", _i, [_sz, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _sz,
@@ -271,6 +272,11 @@ class DeviceSolver:
         if shape is not None and tuple(t.shape) != tuple(shape):
             raise ValueError(f"expected shape {tuple(shape)}, got {tuple(t.shape)}")
         return t
+
+    def set_tuning(self, register_variant=0, blocks_per_sm=0, defer_after=-1):
+        self._check(self.lib.mkpp_set_launch_tuning(C.c_int(register_variant), C.c_int(blocks_per_sm),
+                                                    C.c_int(defer_after)))
+        self._ws = None
 
     def workspace(self, n: int):
         torch = self.torch

@@ -86,13 +86,38 @@ int launch_grid(size_t cells, int block) { return (int)std::max<size_t>(1, (cell
 using StoreInfo = mkpp::StoreFor<Mech>;
 constexpr size_t kQueueBytes = 256;
 
-// Launch configuration of the integrate kernels: the register budget variant
-// (MKPP_MIN_BLOCKS = 1 or 2, see solver.cuh) and the grid, SMs x resident
-// blocks per SM.  MKPP_BLOCKS_PER_SM caps the residency (fewer blocks keep
-// the per-block scratch tiles of large mechanisms closer to L2).
+// Launch configuration of the integrate kernels, process wide:
+//  register_variant  launch-bounds minimum of resident blocks (2: up to 255
+//                    registers per thread, 4: up to 128, more resident warps);
+//  blocks_per_sm     cap on resident blocks per SM (0: as many as fit);
+//  defer_after       attempts within one host step after which the persistent
+//                    kernel parks a cell for the warp-cooperative kernel
+//                    (0: never).
+// Initial values come from MKPP_REGISTER_VARIANT, MKPP_BLOCKS_PER_SM and
+// MKPP_DEFER_AFTER, and mkpp_set_launch_tuning changes them.
+struct Tuning {
+  int register_variant = 2;
+  int blocks_per_sm = 0;
+  int defer_after = 2048;
+};
+
+Tuning& tuning() {
+  static Tuning t = [] {
+    Tuning x;
+    if (const char* e = std::getenv("MKPP_REGISTER_VARIANT")) x.register_variant = std::atoi(e) == 4 ? 4 : 2;
+    if (const char* e = std::getenv("MKPP_BLOCKS_PER_SM")) x.blocks_per_sm = std::max(0, std::atoi(e));
+    if (const char* e = std::getenv("MKPP_DEFER_AFTER")) x.defer_after = std::max(0, std::atoi(e));
+    return x;
+  }();
+  return t;
+}
+
 struct LaunchConfig {
-  int minb = 2;
+  int minb = 0;
   int grid = 0;
+  int sms = 0;
+  int coop_warps = 0;
+  size_t coop_smem = 0;
 };
 
 template <int MINB>
@@ -102,26 +127,40 @@ int resident_blocks() {
   return std::max(1, per_sm);
 }
 
+LaunchConfig g_config;
+
 const LaunchConfig& launch_config() {
-  static LaunchConfig cfg;
+  LaunchConfig& cfg = g_config;
   if (cfg.grid == 0) {
-    int dev = 0, sms = 0;
+    const Tuning& t = tuning();
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (const char* env = std::getenv("MKPP_MIN_BLOCKS")) cfg.minb = std::atoi(env) == 4 ? 4 : 2;
+    cudaDeviceGetAttribute(&cfg.sms, cudaDevAttrMultiProcessorCount, dev);
+    cfg.sms = std::max(1, cfg.sms);
+    cfg.minb = t.register_variant;
     int per_sm = cfg.minb == 4 ? resident_blocks<4>() : resident_blocks<2>();
-    if (const char* env = std::getenv("MKPP_BLOCKS_PER_SM")) {
-      const int cap = std::atoi(env);
-      if (cap > 0) per_sm = std::min(per_sm, cap);
-    }
-    cfg.grid = std::max(1, sms) * per_sm;
+    if (t.blocks_per_sm > 0) per_sm = std::min(per_sm, t.blocks_per_sm);
+    cfg.grid = cfg.sms * per_sm;
+    // Cooperative kernel: as many warps per block as fit in 200 KB of shared memory.
+    const size_t per_warp = (size_t)Mech::COOP_SLOTS * sizeof(double);
+    cfg.coop_warps = (int)std::max<size_t>(1, std::min<size_t>(4, (200u * 1024u) / per_warp));
+    cfg.coop_smem = per_warp * cfg.coop_warps;
+    cudaFuncSetAttribute(mkpp::integrate_coop_kernel<Mech>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cfg.coop_smem);
   }
   return cfg;
 }
 
 int integrate_grid() { return launch_config().grid; }
 
-size_t workspace_bytes() { return kQueueBytes + (size_t)integrate_grid() * StoreInfo::block_bytes; }
+// Workspace layout: [queue counter, parked-cell counter | 256 B]
+// [per-block scratch tiles][parked-cell records, one per cell].
+size_t scratch_offset() { return kQueueBytes; }
+size_t defer_offset() {
+  const size_t end = kQueueBytes + (size_t)integrate_grid() * StoreInfo::block_bytes;
+  return (end + 255) / 256 * 256;
+}
+size_t workspace_bytes(size_t cells) { return defer_offset() + cells * sizeof(mkpp::Deferred); }
 
 int launch_rates(size_t cells, const double* conc, const double* temp, const double* rho,
                  const double* rh, const double* clw, const double* param, double* ktab,
@@ -140,21 +179,29 @@ int launch_rates(size_t cells, const double* conc, const double* temp, const dou
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
 
-// workspace: [queue counter | per-block scratch tiles], workspace_bytes() long.
 int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cudaStream_t stream) {
   mkpp::LaunchArgs a = args;
   unsigned char* ws = (unsigned char*)workspace;
   a.queue = (unsigned int*)ws;
-  double* scratch = StoreInfo::block_bytes ? (double*)(ws + kQueueBytes) : nullptr;
+  a.defer_count = (unsigned int*)ws + 1;
+  double* scratch = StoreInfo::block_bytes ? (double*)(ws + scratch_offset()) : nullptr;
   const LaunchConfig& cfg = launch_config();
+  if (cudaMemsetAsync(ws, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
   if (mode == 1) {
-    if (cudaMemsetAsync(a.queue, 0, sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
+    a.defer_after = tuning().defer_after;
+    a.defer = a.defer_after > 0 ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
+    if (!a.defer) a.defer_after = 0;
     if (cfg.minb == 4)
       mkpp::integrate_persistent_kernel<Mech, 4><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
     else
       mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+    if (a.defer_after > 0) {
+      mkpp::integrate_coop_kernel<Mech><<<cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream>>>(a);
+    }
   } else {
     // The plain form runs with the same grid and the 255-register variant.
+    a.defer = nullptr;
+    a.defer_after = 0;
     mkpp::integrate_plain_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
   }
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
@@ -417,7 +464,7 @@ static int ensure_device(mkpp_handle_s* h, size_t out_bytes) {
     MKPP_CUDA(h, cudaMalloc(&d.status, n * sizeof(int)));
     MKPP_CUDA(h, cudaMalloc(&d.accepted, n * sizeof(int)));
     MKPP_CUDA(h, cudaMalloc(&d.rejected, n * sizeof(int)));
-    MKPP_CUDA(h, cudaMalloc(&d.workspace, workspace_bytes()));
+    MKPP_CUDA(h, cudaMalloc(&d.workspace, workspace_bytes(n)));
     d.cells = n;
   }
   if (out_bytes > d.out_bytes) {
@@ -593,9 +640,17 @@ int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions
 
 // ---- Device-pointer entry points --------------------------------------------
 
-size_t mkpp_gpu_workspace_bytes(size_t num_cells) {
-  (void)num_cells;  // the integrate grid is sized to the GPU, not to the cells
-  return workspace_bytes();
+size_t mkpp_gpu_workspace_bytes(size_t num_cells) { return workspace_bytes(num_cells); }
+
+int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after) {
+  if (register_variant != 0 && register_variant != 2 && register_variant != 4) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (blocks_per_sm < 0 || defer_after < -1) return MKPP_ERROR_INVALID_ARGUMENT;
+  Tuning& t = tuning();
+  if (register_variant) t.register_variant = register_variant;
+  t.blocks_per_sm = blocks_per_sm;
+  if (defer_after >= 0) t.defer_after = defer_after;
+  g_config = LaunchConfig();  // recomputed at the next launch
+  return MKPP_SUCCESS;
 }
 
 int mkpp_gpu_rate_constants(size_t num_cells, const double* conc, const double* temp, const double* rho,
@@ -613,7 +668,7 @@ static int check_integrate_args(size_t num_cells, const double* conc, const doub
   if (!conc || !ktab || !workspace) return MKPP_ERROR_NULL_POINTER;
   if (num_cells == 0 || num_cells > (size_t)INT32_MAX) return MKPP_ERROR_INVALID_ARGUMENT;
   if (!std::isfinite(dt) || dt <= 0.0 || steps < 1 || !(seed > 0.0) || max_attempts < 1) return MKPP_ERROR_INVALID_ARGUMENT;
-  if (workspace_bytes_ < workspace_bytes()) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (workspace_bytes_ < workspace_bytes(num_cells)) return MKPP_ERROR_INVALID_ARGUMENT;
   if (((uintptr_t)workspace) % 256 != 0) return MKPP_ERROR_INVALID_ARGUMENT;
   return MKPP_SUCCESS;
 }

@@ -36,12 +36,24 @@ struct LaunchArgs {
   int* n_reject;             // [ncells] or null
   unsigned int* queue;       // persistent kernel work counter (zeroed before launch)
   const int* order;          // persistent kernel: queue position -> cell, or null (identity)
+  // Hand-off of slow cells to the warp-cooperative kernel: a cell whose
+  // attempts within one host step reach defer_after (> 0) is parked in
+  // defer[] (controller state) with its state written back to conc.
+  struct Deferred* defer;
+  unsigned int* defer_count;
+  int defer_after;
   // Optional per-attempt log for step-sequence replay in the CPU oracle:
   // entry a of cell c at [a * ncells + c]; log_n[c] = attempts recorded.
   double* log_h;
   unsigned char* log_acc;
   int* log_n;
   int log_cap;
+};
+
+// Controller state of a parked cell (see LaunchArgs::defer).
+struct Deferred {
+  int cell, step, attempts, nacc, nrej, flags;  // flags: 1 reject_last, 2 reject_more, 4 zero pivot
+  double t, dt;
 };
 
 struct RateArgs {
@@ -339,6 +351,22 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         if (!ctl.running()) {
           if (++step < a.steps) ctl.start(a.dt, a.seed);
           else done = true;
+        } else if (a.defer_after > 0 && ctl.attempts >= a.defer_after) {
+          // Too slow for one lane: park the cell for the cooperative kernel.
+          const unsigned slot = atomicAdd(a.defer_count, 1u);
+          Deferred d;
+          d.cell = (int)cell;
+          d.step = step;
+          d.attempts = ctl.attempts;
+          d.nacc = nacc;
+          d.nrej = nrej;
+          d.flags = (ctl.reject_last ? 1 : 0) | (ctl.reject_more ? 2 : 0) | (zero_pivot ? 4 : 0);
+          d.t = ctl.t;
+          d.dt = ctl.dt;
+          a.defer[slot] = d;
+          store_state<Mech>(a.conc, (size_t)cell, n, S);
+          cell = -1;
+          continue;
         }
       }
     }
@@ -352,6 +380,75 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
       }
       cell = -1;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cooperative form for parked cells: a whole warp integrates one cell at a
+// time, the cell's working set in shared memory, each attempt spread over
+// the lanes by the level schedules of Mech::attempt_coop.  It resumes the
+// parked controller state exactly, and attempt_coop reproduces attempt's
+// arithmetic, so a parked cell ends bit-identical to an unparked one.
+// ---------------------------------------------------------------------------
+constexpr int kCoopWarps = 4;
+
+template <class Mech>
+__global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(LaunchArgs a) {
+  extern __shared__ double smem[];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned wib = threadIdx.x >> 5;
+  double* S = smem + (size_t)wib * Mech::COOP_SLOTS;
+  const size_t n = (size_t)a.ncells;
+  const unsigned count = *a.defer_count;
+  for (unsigned idx = blockIdx.x * kCoopWarps + wib; idx < count; idx += gridDim.x * kCoopWarps) {
+    const Deferred d = a.defer[idx];
+    const size_t c = (size_t)d.cell;
+    for (int i = lane; i < Mech::NV; i += 32) S[Mech::Y + i] = a.conc[c + n * Mech::var_phys(i)];
+    __syncwarp();
+    Controller ctl;
+    ctl.start(a.dt, a.seed);
+    ctl.t = d.t;
+    ctl.dt = d.dt;
+    ctl.attempts = d.attempts;
+    ctl.reject_last = d.flags & 1;
+    ctl.reject_more = (d.flags & 2) != 0;
+    bool zero_pivot = (d.flags & 4) != 0, capped = false;
+    int nacc = d.nacc, nrej = d.nrej;
+    for (int step = d.step; step < a.steps;) {
+      const KTable k{a.ktab + (size_t)step * a.k_step_stride + c, n};
+      while (ctl.running()) {
+        if (ctl.attempts >= a.max_attempts) {
+          capped = true;
+          break;
+        }
+        const double h = ctl.next_h();
+        int st = 0;
+        const double err = Mech::attempt_coop(S, k, h, st, lane);
+        zero_pivot |= st != 0;
+        if (ctl.update<Mech>(err)) {
+          for (int i = lane; i < Mech::NV; i += 32) S[Mech::Y + i] += S[Mech::DY + i];
+          __syncwarp();
+          ++nacc;
+        } else {
+          ++nrej;
+        }
+      }
+      if (capped || ++step >= a.steps) break;
+      ctl.start(a.dt, a.seed);
+    }
+    bool fin = true;
+    for (int i = lane; i < Mech::NV; i += 32) fin = fin && finite(S[Mech::Y + i]);
+    fin = __all_sync(0xffffffffu, fin);
+    for (int i = lane; i < Mech::NV; i += 32) a.conc[c + n * Mech::var_phys(i)] = S[Mech::Y + i];
+    if (lane == 0) {
+      const int status = !fin ? CELL_ERR_NUMERICAL_FAILURE
+                              : (capped ? CELL_ERR_CONVERGENCE_FAILURE
+                                        : (zero_pivot ? CELL_ERR_SINGULAR_MATRIX : CELL_SUCCESS));
+      if (a.status) a.status[c] = status;
+      if (a.n_accept) a.n_accept[c] = nacc;
+      if (a.n_reject) a.n_reject[c] = nrej;
+    }
+    __syncwarp();
   }
 }
 

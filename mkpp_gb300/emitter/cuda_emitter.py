@@ -124,6 +124,351 @@ def _interleave(c, plan, ops, operands, scale):
                 c(f"      S[{out}] = v{out};")
 
 
+def _levels(deps_of, n):
+    """Longest-path level of items 0..n-1 given deps_of(i) (earlier items)."""
+    lev = [0] * n
+    for i in range(n):
+        d = deps_of(i)
+        lev[i] = 1 + max((lev[j] for j in d), default=-1)
+    return lev
+
+
+def _c_array(c, ctype, name, values):
+    vals = list(values) or [0]
+    body = ", ".join(str(v) for v in vals)
+    c(f"static __device__ const {ctype} {name}[{len(vals)}] = {{{body}}};")
+
+
+def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None):
+    """Warp-cooperative form of one attempt: the same arithmetic, element by
+    element, as ``attempt`` (same operand order in every sum and product), with
+    the independent elements of each phase spread over the 32 lanes of a warp.
+    Used for the few cells whose step count makes one lane too slow."""
+    v2l = plan.phys_to_var
+    nr = len(plan.reactions)
+    # --- rates q_r = k_r * y ... (factor order of fun)
+    r_off, r_y = [0], []
+    for r in plan.reactions:
+        for s_, pw in r.reactants:
+            r_y += [v2l[s_]] * pw
+        r_off.append(len(r_y))
+    # --- F_i = sum over reactions (order of fun)
+    f_off, f_r, f_c = [0], [], []
+    contrib = {i: [] for i in range(nv)}
+    for r in plan.reactions:
+        for s_, coef in r.net:
+            contrib[v2l[s_]].append((coef, r.index))
+    for i in range(nv):
+        for coef, ri in contrib[i]:
+            f_r.append(ri)
+            f_c.append(_lit(coef))
+        f_off.append(len(f_r))
+    # --- partials d = k * [pw] * y ... (factor order of jac_w); factor -1 = the literal pw
+    d_r, d_off, d_fac, d_lit = [], [0], [], []
+    pidx = {}
+    for r in plan.reactions:
+        terms = list(r.reactants)
+        for idx, (s_, pw) in enumerate(terms):
+            fac = []
+            lit = 1.0
+            for jdx, (s2, pw2) in enumerate(terms):
+                if jdx == idx:
+                    if pw2 > 1:
+                        fac.append(-1)
+                        lit = float(pw2)
+                        fac += [v2l[s2]] * (pw2 - 1)
+                else:
+                    fac += [v2l[s2]] * pw2
+            pidx[(r.index, s_)] = len(d_r)
+            d_r.append(r.index)
+            d_fac += fac
+            d_lit.append(_lit(lit))
+            d_off.append(len(d_fac))
+    npart = len(d_r)
+    # --- W slots: init (diag) + terms (coef, partial) in jac_w order
+    w_slot, w_diag, w_off, w_p, w_c = [], [], [0], [], []
+    wterms = {loc: [] for loc in plan.w_slots}
+    for r in plan.reactions:
+        for s_, coef in r.net:
+            for s2, _pw in r.reactants:
+                wterms[(v2l[s_], v2l[s2])].append((-coef, pidx[(r.index, s2)]))
+    for loc in plan.w_slots:
+        w_slot.append(plan.lu_index[loc])
+        w_diag.append(int(loc[0] == loc[1]))
+        for coef, pi in wterms[loc]:
+            w_p.append(pi)
+            w_c.append(_lit(coef))
+        w_off.append(len(w_p))
+    # --- LU ops by level; kind 0 = plain, 1 = pivot (store 1/u), 2 = L (times 1/U_jj)
+    diag_slots = set(plan.diag)
+    slot_level = {}
+    op_level = []
+    for out, w, b, e, dg in plan.ops:
+        deps = [slot_level[x] for q in range(b, e) for x in plan.products[q]]
+        if dg >= 0:
+            deps.append(slot_level[dg])
+        L = 1 + max(deps) if deps else 0
+        slot_level[out] = L
+        op_level.append(L)
+    nlev = max(op_level) + 1
+    order = sorted(range(len(plan.ops)), key=lambda i: (op_level[i], -(plan.ops[i][3] - plan.ops[i][2]), i))
+    lu_lev_off = [0] * (nlev + 1)
+    for i in order:
+        lu_lev_off[op_level[i] + 1] += 1
+    for l in range(nlev):
+        lu_lev_off[l + 1] += lu_lev_off[l]
+    op_out, op_w, op_b, op_e, op_kind, op_dg = [], [], [], [], [], []
+    for i in order:
+        out, w, b, e, dg = plan.ops[i]
+        op_out.append(out)
+        op_w.append(int(w >= 0))
+        op_b.append(b)
+        op_e.append(e)
+        op_kind.append(1 if out in diag_slots else (2 if dg >= 0 else 0))
+        op_dg.append(dg if dg >= 0 else 0)
+    prod_l = [a for a, _ in plan.products]
+    prod_r = [b for _, b in plan.products]
+    # --- solves by level
+    fl = _levels(lambda i: [cc for cc, _ in plan.lower[i]], nv)
+    nfl = max(fl) + 1
+    bl_rev = [0] * nv
+    for i in range(nv - 1, -1, -1):
+        bl_rev[i] = 1 + max((bl_rev[cc] for cc, _ in plan.upper[i]), default=-1)
+    nbl = max(bl_rev) + 1
+    def lev_rows(levs, nl):
+        rows = sorted(range(nv), key=lambda i: (levs[i], i))
+        off = [0] * (nl + 1)
+        for i in rows:
+            off[levs[i] + 1] += 1
+        for l in range(nl):
+            off[l + 1] += off[l]
+        return rows, off
+    f_rows, f_lev_off = lev_rows(fl, nfl)
+    b_rows, b_lev_off = lev_rows(bl_rev, nbl)
+    lo_off, lo_col, lo_slot, up_off, up_col, up_slot = [0], [], [], [0], [], []
+    for i in range(nv):
+        for cc, sl in plan.lower[i]:
+            lo_col.append(cc)
+            lo_slot.append(sl)
+        lo_off.append(len(lo_col))
+        for cc, sl in plan.upper[i]:
+            up_col.append(cc)
+            up_slot.append(sl)
+        up_off.append(len(up_col))
+    c("")
+    c("  // ---- warp-cooperative attempt (tables + level schedules) ----")
+    c(f"  static constexpr int NPART = {npart};")
+    nq = max(nr, nv)
+    c(f"  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm")
+    c(f"  static constexpr int D = NSLOTS + {nq};     // partial derivatives")
+    c(f"  static constexpr int COOP_SLOTS = NSLOTS + {nq} + NPART;")
+    t = _Code()
+    t("// Tables of the warp-cooperative attempt (device constant data).")
+    t("namespace coop {")
+    c_ = c
+    c = t
+    _c_array(c, "int", "r_off", r_off)
+    _c_array(c, "int", "r_y", r_y)
+    _c_array(c, "int", "f_off", f_off)
+    _c_array(c, "int", "f_r", f_r)
+    _c_array(c, "double", "f_c", f_c)
+    _c_array(c, "int", "d_r", d_r)
+    _c_array(c, "int", "d_off", d_off)
+    _c_array(c, "int", "d_fac", d_fac)
+    _c_array(c, "double", "d_lit", d_lit)
+    _c_array(c, "int", "w_slot", w_slot)
+    _c_array(c, "int", "w_diag", w_diag)
+    _c_array(c, "int", "w_off", w_off)
+    _c_array(c, "int", "w_p", w_p)
+    _c_array(c, "double", "w_c", w_c)
+    c(f"constexpr int LU_LEVELS = {nlev};")
+    c(f"constexpr int NW = {len(w_slot)};")
+    _c_array(c, "int", "lu_lev_off", lu_lev_off)
+    _c_array(c, "int", "op_out", op_out)
+    _c_array(c, "int", "op_w", op_w)
+    _c_array(c, "int", "op_b", op_b)
+    _c_array(c, "int", "op_e", op_e)
+    _c_array(c, "int", "op_kind", op_kind)
+    _c_array(c, "int", "op_dg", op_dg)
+    _c_array(c, "int", "prod_l", prod_l)
+    _c_array(c, "int", "prod_r", prod_r)
+    c(f"constexpr int F_LEVELS = {nfl};")
+    c(f"constexpr int B_LEVELS = {nbl};")
+    _c_array(c, "int", "f_rows", f_rows)
+    _c_array(c, "int", "f_lev_off", f_lev_off)
+    _c_array(c, "int", "b_rows", b_rows)
+    _c_array(c, "int", "b_lev_off", b_lev_off)
+    _c_array(c, "int", "lo_off", lo_off)
+    _c_array(c, "int", "lo_col", lo_col)
+    _c_array(c, "int", "lo_slot", lo_slot)
+    _c_array(c, "int", "up_off", up_off)
+    _c_array(c, "int", "up_col", up_col)
+    _c_array(c, "int", "up_slot", up_slot)
+    _c_array(c, "int", "diag", plan.diag)
+    c("}  // namespace coop")
+    c("")
+    c = c_
+    plan._coop_tables = t.text()
+    # accumulate like _accumulate: first term c=1 -> t, c=-1 -> -t, else c*t; then +,-,fma
+    c("  __device__ __forceinline__ static double acc_term(bool first, double acc, double coef, double t) {")
+    c("    if (first) return coef == 1.0 ? t : (coef == -1.0 ? -t : coef * t);")
+    c("    return coef == 1.0 ? acc + t : (coef == -1.0 ? acc - t : fma(coef, t, acc));")
+    c("  }")
+    c("")
+    c("  // F(y) into S[F..] for the state yv (S[Y..] or the stage state), cooperatively.")
+    c("  template <class KA>")
+    c("  __device__ __forceinline__ static void fun_coop(double* S, const double* yv, const KA& k, unsigned lane) {")
+    c("    namespace T = coop;")
+    c("    for (int r = lane; r < NR; r += 32) {")
+    c("      double q = k(r);")
+    c("      for (int e = T::r_off[r]; e < T::r_off[r + 1]; ++e) q = q * yv[T::r_y[e]];")
+    c("      S[Q + r] = q;")
+    c("    }")
+    c("    __syncwarp();")
+    c("    for (int i = lane; i < NV; i += 32) {")
+    c("      double v = 0.0;")
+    c("      for (int e = T::f_off[i]; e < T::f_off[i + 1]; ++e) v = acc_term(e == T::f_off[i], v, T::f_c[e], S[Q + T::f_r[e]]);")
+    c("      S[F + i] = v;")
+    c("    }")
+    c("    __syncwarp();")
+    c("  }")
+    c("")
+    c("  // Solve (LU) x = b in place on S[base..] by dependency levels.")
+    c("  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {")
+    c("    namespace T = coop;")
+    c("    for (int l = 0; l < T::F_LEVELS; ++l) {")
+    c("      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {")
+    c("        const int i = T::f_rows[j];")
+    c("        double v = S[base + i];")
+    c("        for (int e = T::lo_off[i]; e < T::lo_off[i + 1]; ++e) v = fma(-S[T::lo_slot[e]], S[base + T::lo_col[e]], v);")
+    c("        S[base + i] = v;")
+    c("      }")
+    c("      __syncwarp();")
+    c("    }")
+    c("    for (int l = 0; l < T::B_LEVELS; ++l) {")
+    c("      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {")
+    c("        const int i = T::b_rows[j];")
+    c("        double v = S[base + i];")
+    c("        for (int e = T::up_off[i]; e < T::up_off[i + 1]; ++e) v = fma(-S[T::up_slot[e]], S[base + T::up_col[e]], v);")
+    c("        S[base + i] = v * S[T::diag[i]];")
+    c("      }")
+    c("      __syncwarp();")
+    c("    }")
+    c("  }")
+    c("")
+    c("  // One attempt by a whole warp on the cell held in shared memory S")
+    c("  // (NSLOTS + NR + NPART doubles).  Same values as attempt(); the error norm")
+    c("  // is summed by lane 0 in species order.  Returns err on every lane.")
+    c("  template <class KA>")
+    c("  __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,")
+    c("                                                       unsigned lane) {")
+    c("    namespace T = coop;")
+    c("    const double inv_g_dt = 1.0 / (GAMMA * h);")
+    c("    // Jacobian partials, then W into the LU slots.")
+    c("    for (int p = lane; p < NPART; p += 32) {")
+    c("      double d = k(T::d_r[p]);")
+    c("      for (int e = T::d_off[p]; e < T::d_off[p + 1]; ++e) {")
+    c("        const int f = T::d_fac[e];")
+    c("        d = d * (f < 0 ? T::d_lit[p] : S[Y + f]);")
+    c("      }")
+    c("      S[D + p] = d;")
+    c("    }")
+    c("    __syncwarp();")
+    c("    for (int w = lane; w < T::NW; w += 32) {")
+    c("      bool first = !T::w_diag[w];")
+    c("      double v = T::w_diag[w] ? inv_g_dt : 0.0;")
+    c("      for (int e = T::w_off[w]; e < T::w_off[w + 1]; ++e) {")
+    c("        v = acc_term(first, v, T::w_c[e], S[D + T::w_p[e]]);")
+    c("        first = false;")
+    c("      }")
+    c("      S[T::w_slot[w]] = v;")
+    c("    }")
+    c("    __syncwarp();")
+    c("    // LU by dependency levels.")
+    c("    bool ok = true;")
+    c("    for (int l = 0; l < T::LU_LEVELS; ++l) {")
+    c("      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {")
+    c("        const int out = T::op_out[j];")
+    c("        double v = T::op_w[j] ? S[out] : 0.0;")
+    c("        for (int q = T::op_b[j]; q < T::op_e[j]; ++q) v = fma(-S[T::prod_l[q]], S[T::prod_r[q]], v);")
+    c("        const int kind = T::op_kind[j];")
+    c("        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }")
+    c("        else if (kind == 2) S[out] = v * S[T::op_dg[j]];")
+    c("        else S[out] = v;")
+    c("      }")
+    c("      __syncwarp();")
+    c("    }")
+    c("    if (__any_sync(0xffffffffu, !ok)) status |= 1;")
+    cur_f = None
+    for st in range(1, stages + 1):
+        kb = K0 + (st - 1) * nv
+        if NewF[st - 1]:
+            if st == 1:
+                c("    fun_coop(S, S + Y, k, lane);")
+            else:
+                terms = []
+                for j in range(1, st):
+                    a = A[(st - 1) * (st - 2) // 2 + j - 1]
+                    if a != 0.0:
+                        terms.append((a, j))
+                expr = "S[Y + i]"
+                for a, j in terms:
+                    kk = f"S[{K0 + (j - 1) * nv} + i]"
+                    expr = f"{expr} + {kk}" if a == 1.0 else f"{expr} + {_lit(a)} * {kk}"
+                c("    // Stage state into the DY slots (free until the error block).")
+                c(f"    for (int i = lane; i < NV; i += 32) S[DY + i] = {expr};")
+                c("    __syncwarp();")
+                c("    fun_coop(S, S + DY, k, lane);")
+        cterms = []
+        if st > 1:
+            for j in range(1, st):
+                cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+                if cv != 0.0:
+                    cterms.append((cv, j))
+        for cv, j in cterms:
+            c(f"    const double c{st}{j} = {_lit(cv)} / h;")
+        expr = "S[F + i]"
+        for cv, j in cterms:
+            expr = f"fma(c{st}{j}, S[{K0 + (j - 1) * nv} + i], {expr})"
+        c(f"    for (int i = lane; i < NV; i += 32) S[{kb} + i] = {expr};")
+        c("    __syncwarp();")
+        c(f"    solve_coop(S, {kb}, lane);")
+    mterms = [(M[j], j) for j in range(stages) if M[j] != 0.0]
+    eterms = [(E[j], j) for j in range(stages) if E[j] != 0.0]
+
+    def lin(terms):
+        expr = None
+        for cv, j in terms:
+            t = f"k{j}"
+            if expr is None:
+                expr = t if cv == 1.0 else f"{_lit(cv)} * {t}"
+            else:
+                expr = f"{expr} + {t}" if cv == 1.0 else f"fma({_lit(cv)}, {t}, {expr})"
+        return expr or "0.0"
+    c("    // Increment, and q_i^2 of the error norm into the rate slots.")
+    c("    for (int i = lane; i < NV; i += 32) {")
+    for j in range(stages):
+        c(f"      const double k{j} = S[{K0 + j * nv} + i];")
+    c("      const double yi = S[Y + i];")
+    ynew = "yi"
+    for cv, j in mterms:
+        ynew = f"{ynew} + k{j}" if cv == 1.0 else f"fma({_lit(cv)}, k{j}, {ynew})"
+    c(f"      const double ynew = {ynew};")
+    c(f"      S[DY + i] = {lin(mterms)};")
+    c("      const double sc = fma(rtol_v(i), fmax(fabs(yi), fabs(ynew)), atol_v(i));")
+    c(f"      S[Q + i] = ({lin(eterms)}) / sc;")
+    c("    }")
+    c("    __syncwarp();")
+    c("    double err = 0.0;")
+    c("    if (lane == 0) {")
+    c("      double err_sq = 0.0;")
+    c("      for (int i = 0; i < NV; ++i) err_sq = fma(S[Q + i], S[Q + i], err_sq);")
+    c(f"      err = fmax(sqrt(err_sq / {ns}.0), 1.0e-10);")
+    c("    }")
+    c("    return __shfl_sync(0xffffffffu, err, 0);")
+    c("  }")
+
+
 def emit_mechanism(plan: ReducedPlan) -> str:
     raw = plan.raw
     name = plan.name
@@ -469,10 +814,12 @@ def emit_mechanism(plan: ReducedPlan) -> str:
         c(f"    const double fac = 0.9 * pow(err, -{_lit(1.0 / elo)});")
     c("    return fmax(0.2, fmin(fac, 6.0));")
     c("  }")
+    _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None)
     c("};")
     c("")
     c(f"}}  // namespace mkpp_{name}")
-    return c.text()
+    text = c.text()
+    return text.replace("struct Mech {", plan._coop_tables + "\nstruct Mech {", 1)
 
 
 def write(name: str, out_dir: Path = GEN_DIR) -> Path:

@@ -5,6 +5,49 @@
 #include "mkpp_device.cuh"
 namespace mkpp_small_strato {
 
+// Tables of the warp-cooperative attempt (device constant data).
+namespace coop {
+static __device__ const int r_off[11] = {0, 1, 3, 4, 6, 7, 8, 10, 12, 14, 15};
+static __device__ const int r_y[15] = {2, 1, 2, 3, 1, 3, 3, 0, 0, 3, 4, 3, 5, 1, 5};
+static __device__ const int f_off[7] = {0, 3, 10, 18, 24, 27, 30};
+static __device__ const int f_r[30] = {4, 5, 6, 0, 1, 2, 3, 5, 8, 9, 0, 1, 2, 3, 4, 6, 7, 8, 1, 2, 3, 4, 6, 7, 7, 8, 9, 7, 8, 9};
+static __device__ const double f_c[30] = {1.0, -1.0, -1.0, 2.0, -1.0, 1.0, -1.0, 1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 2.0, 1.0, 2.0, 1.0, 1.0, 1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, -1.0, -1.0};
+static __device__ const int d_r[15] = {0, 1, 1, 2, 3, 3, 4, 5, 6, 6, 7, 7, 8, 8, 9};
+static __device__ const int d_off[16] = {0, 0, 1, 2, 2, 3, 4, 4, 4, 5, 6, 7, 8, 9, 10, 10};
+static __device__ const int d_fac[10] = {2, 1, 3, 1, 3, 0, 3, 4, 1, 5};
+static __device__ const double d_lit[15] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
+static __device__ const int w_slot[26] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 19, 21, 22, 23, 24, 26, 27, 28};
+static __device__ const int w_diag[26] = {1, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+static __device__ const int w_off[27] = {0, 2, 4, 5, 8, 10, 12, 14, 15, 18, 20, 25, 26, 27, 28, 30, 31, 36, 37, 38, 39, 40, 42, 43, 44, 45, 47};
+static __device__ const int w_p[47] = {7, 8, 6, 9, 7, 1, 4, 13, 0, 2, 3, 5, 12, 14, 8, 1, 4, 13, 0, 2, 3, 5, 6, 9, 11, 10, 12, 8, 1, 4, 2, 3, 5, 6, 9, 11, 10, 13, 11, 10, 12, 14, 13, 11, 10, 12, 14};
+static __device__ const double w_c[47] = {1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, -2.0, 1.0, -1.0, 1.0, 1.0, -1.0, -2.0, 1.0, -2.0, -1.0, 1.0, 1.0, -1.0, -2.0, -1.0, -2.0, -1.0, -1.0, -1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, -1.0, 1.0, 1.0, -1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 1.0};
+constexpr int LU_LEVELS = 9;
+constexpr int NW = 26;
+static __device__ const int lu_lev_off[10] = {0, 6, 13, 16, 20, 23, 25, 27, 28, 29};
+static __device__ const int op_out[29] = {0, 1, 3, 4, 6, 11, 2, 7, 13, 8, 14, 19, 24, 5, 9, 12, 10, 15, 20, 25, 16, 18, 17, 21, 26, 23, 22, 27, 28};
+static __device__ const int op_w[29] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 1, 0, 1, 1, 1, 1, 1, 1, 1};
+static __device__ const int op_b[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 0, 1, 4, 2, 5, 6, 7, 8, 12, 11, 14, 16, 20, 18, 23, 25};
+static __device__ const int op_e[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 1, 2, 5, 4, 6, 7, 8, 11, 14, 12, 16, 18, 23, 20, 25, 29};
+static __device__ const int op_kind[29] = {1, 0, 1, 0, 0, 0, 2, 2, 2, 2, 2, 2, 2, 0, 1, 0, 0, 2, 2, 2, 1, 0, 0, 2, 2, 0, 1, 2, 1};
+static __device__ const int op_dg[29] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 3, 3, 3, 3, 0, 0, 0, 0, 9, 9, 9, 0, 0, 0, 16, 16, 0, 0, 22, 0};
+static __device__ const int prod_l[29] = {2, 8, 7, 8, 8, 14, 19, 24, 13, 14, 15, 15, 14, 15, 19, 20, 24, 25, 20, 21, 19, 20, 21, 25, 26, 24, 25, 26, 27};
+static __device__ const int prod_r[29] = {1, 4, 1, 5, 6, 4, 4, 4, 1, 5, 10, 11, 6, 12, 5, 10, 5, 10, 11, 17, 6, 12, 18, 11, 17, 6, 12, 18, 23};
+constexpr int F_LEVELS = 6;
+constexpr int B_LEVELS = 5;
+static __device__ const int f_rows[6] = {0, 1, 2, 3, 4, 5};
+static __device__ const int f_lev_off[7] = {0, 1, 2, 3, 4, 5, 6};
+static __device__ const int b_rows[6] = {5, 4, 3, 0, 2, 1};
+static __device__ const int b_lev_off[6] = {0, 1, 2, 3, 5, 6};
+static __device__ const int lo_off[7] = {0, 0, 1, 3, 6, 9, 13};
+static __device__ const int lo_col[13] = {0, 0, 1, 0, 1, 2, 1, 2, 3, 1, 2, 3, 4};
+static __device__ const int lo_slot[13] = {2, 7, 8, 13, 14, 15, 19, 20, 21, 24, 25, 26, 27};
+static __device__ const int up_off[7] = {0, 1, 4, 7, 9, 10, 10};
+static __device__ const int up_col[10] = {3, 2, 3, 5, 3, 4, 5, 4, 5, 5};
+static __device__ const int up_slot[10] = {1, 4, 5, 6, 10, 11, 12, 17, 18, 23};
+static __device__ const int diag[6] = {0, 3, 9, 16, 22, 28};
+}  // namespace coop
+
+
 struct Mech {
   static constexpr const char* NAME = "small_strato";
   static constexpr int NS = 7;      // species including fixed ones
@@ -385,6 +428,138 @@ struct Mech {
   __device__ __forceinline__ static double growth(double err) {
     const double fac = 0.9 / cbrt(err);
     return fmax(0.2, fmin(fac, 6.0));
+  }
+
+  // ---- warp-cooperative attempt (tables + level schedules) ----
+  static constexpr int NPART = 15;
+  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
+  static constexpr int D = NSLOTS + 10;     // partial derivatives
+  static constexpr int COOP_SLOTS = NSLOTS + 10 + NPART;
+  __device__ __forceinline__ static double acc_term(bool first, double acc, double coef, double t) {
+    if (first) return coef == 1.0 ? t : (coef == -1.0 ? -t : coef * t);
+    return coef == 1.0 ? acc + t : (coef == -1.0 ? acc - t : fma(coef, t, acc));
+  }
+
+  // F(y) into S[F..] for the state yv (S[Y..] or the stage state), cooperatively.
+  template <class KA>
+  __device__ __forceinline__ static void fun_coop(double* S, const double* yv, const KA& k, unsigned lane) {
+    namespace T = coop;
+    for (int r = lane; r < NR; r += 32) {
+      double q = k(r);
+      for (int e = T::r_off[r]; e < T::r_off[r + 1]; ++e) q = q * yv[T::r_y[e]];
+      S[Q + r] = q;
+    }
+    __syncwarp();
+    for (int i = lane; i < NV; i += 32) {
+      double v = 0.0;
+      for (int e = T::f_off[i]; e < T::f_off[i + 1]; ++e) v = acc_term(e == T::f_off[i], v, T::f_c[e], S[Q + T::f_r[e]]);
+      S[F + i] = v;
+    }
+    __syncwarp();
+  }
+
+  // Solve (LU) x = b in place on S[base..] by dependency levels.
+  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {
+    namespace T = coop;
+    for (int l = 0; l < T::F_LEVELS; ++l) {
+      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {
+        const int i = T::f_rows[j];
+        double v = S[base + i];
+        for (int e = T::lo_off[i]; e < T::lo_off[i + 1]; ++e) v = fma(-S[T::lo_slot[e]], S[base + T::lo_col[e]], v);
+        S[base + i] = v;
+      }
+      __syncwarp();
+    }
+    for (int l = 0; l < T::B_LEVELS; ++l) {
+      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {
+        const int i = T::b_rows[j];
+        double v = S[base + i];
+        for (int e = T::up_off[i]; e < T::up_off[i + 1]; ++e) v = fma(-S[T::up_slot[e]], S[base + T::up_col[e]], v);
+        S[base + i] = v * S[T::diag[i]];
+      }
+      __syncwarp();
+    }
+  }
+
+  // One attempt by a whole warp on the cell held in shared memory S
+  // (NSLOTS + NR + NPART doubles).  Same values as attempt(); the error norm
+  // is summed by lane 0 in species order.  Returns err on every lane.
+  template <class KA>
+  __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,
+                                                       unsigned lane) {
+    namespace T = coop;
+    const double inv_g_dt = 1.0 / (GAMMA * h);
+    // Jacobian partials, then W into the LU slots.
+    for (int p = lane; p < NPART; p += 32) {
+      double d = k(T::d_r[p]);
+      for (int e = T::d_off[p]; e < T::d_off[p + 1]; ++e) {
+        const int f = T::d_fac[e];
+        d = d * (f < 0 ? T::d_lit[p] : S[Y + f]);
+      }
+      S[D + p] = d;
+    }
+    __syncwarp();
+    for (int w = lane; w < T::NW; w += 32) {
+      bool first = !T::w_diag[w];
+      double v = T::w_diag[w] ? inv_g_dt : 0.0;
+      for (int e = T::w_off[w]; e < T::w_off[w + 1]; ++e) {
+        v = acc_term(first, v, T::w_c[e], S[D + T::w_p[e]]);
+        first = false;
+      }
+      S[T::w_slot[w]] = v;
+    }
+    __syncwarp();
+    // LU by dependency levels.
+    bool ok = true;
+    for (int l = 0; l < T::LU_LEVELS; ++l) {
+      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {
+        const int out = T::op_out[j];
+        double v = T::op_w[j] ? S[out] : 0.0;
+        for (int q = T::op_b[j]; q < T::op_e[j]; ++q) v = fma(-S[T::prod_l[q]], S[T::prod_r[q]], v);
+        const int kind = T::op_kind[j];
+        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }
+        else if (kind == 2) S[out] = v * S[T::op_dg[j]];
+        else S[out] = v;
+      }
+      __syncwarp();
+    }
+    if (__any_sync(0xffffffffu, !ok)) status |= 1;
+    fun_coop(S, S + Y, k, lane);
+    for (int i = lane; i < NV; i += 32) S[35 + i] = S[F + i];
+    __syncwarp();
+    solve_coop(S, 35, lane);
+    // Stage state into the DY slots (free until the error block).
+    for (int i = lane; i < NV; i += 32) S[DY + i] = S[Y + i] + S[35 + i];
+    __syncwarp();
+    fun_coop(S, S + DY, k, lane);
+    const double c21 = -1.0156171083877703 / h;
+    for (int i = lane; i < NV; i += 32) S[41 + i] = fma(c21, S[35 + i], S[F + i]);
+    __syncwarp();
+    solve_coop(S, 41, lane);
+    const double c31 = 4.0759956452537702 / h;
+    const double c32 = 9.20767942983308 / h;
+    for (int i = lane; i < NV; i += 32) S[47 + i] = fma(c32, S[41 + i], fma(c31, S[35 + i], S[F + i]));
+    __syncwarp();
+    solve_coop(S, 47, lane);
+    // Increment, and q_i^2 of the error norm into the rate slots.
+    for (int i = lane; i < NV; i += 32) {
+      const double k0 = S[35 + i];
+      const double k1 = S[41 + i];
+      const double k2 = S[47 + i];
+      const double yi = S[Y + i];
+      const double ynew = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, yi + k0));
+      S[DY + i] = fma(-0.42772256543218573, k2, fma(6.1697947043828245, k1, k0));
+      const double sc = fma(rtol_v(i), fmax(fabs(yi), fabs(ynew)), atol_v(i));
+      S[Q + i] = (fma(0.22354069897811571, k2, fma(-2.9079558716805471, k1, 0.5 * k0))) / sc;
+    }
+    __syncwarp();
+    double err = 0.0;
+    if (lane == 0) {
+      double err_sq = 0.0;
+      for (int i = 0; i < NV; ++i) err_sq = fma(S[Q + i], S[Q + i], err_sq);
+      err = fmax(sqrt(err_sq / 7.0), 1.0e-10);
+    }
+    return __shfl_sync(0xffffffffu, err, 0);
   }
 };
 

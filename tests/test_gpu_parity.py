@@ -261,3 +261,25 @@ def test_windowed_launch_equals_per_step_launches(built_libs):
     torch.cuda.synchronize()
     assert torch.equal(a, b)
     assert int(st.sum()) == 0
+
+
+@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99"])
+@pytest.mark.parametrize("defer_after", [1, 7])
+def test_cooperative_handoff_is_bit_identical(built_libs, mech, defer_after):
+    """Cells parked after `defer_after` attempts and finished by the
+    warp-cooperative kernel end exactly as cells that stay on one lane."""
+    torch = _torch()
+    w, s, o = _setup(mech, 96 if mech == "saprc99" else 512)
+    outs = []
+    try:
+        for d in (0, defer_after):
+            s.set_tuning(defer_after=d)
+            conc = _dev(w.conc)
+            st, acc, rej = s.integrate(conc, w.dt, temp=_dev(w.temp), rho=_dev(w.rho), rh=_dev(w.rh),
+                                       param=_dev(w.param), mode="persistent")
+            torch.cuda.synchronize()
+            outs.append((conc.cpu().numpy(), st.cpu().numpy(), acc.cpu().numpy(), rej.cpu().numpy()))
+    finally:
+        s.set_tuning(defer_after=2048)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b, equal_nan=True)
