@@ -111,8 +111,8 @@ size_t mkpp_gpu_workspace_bytes(size_t num_cells);
 /* Process-wide launch tuning of the integrate kernels (the autotuner's
  * knobs): register_variant 2 (up to 255 registers per thread) or 4 (up to
  * 128, more resident warps), 0 keeps the current one; blocks_per_sm caps the
- * resident blocks per SM (0: as many as fit); defer_after: attempts within one
- * host step after which the persistent kernel hands a cell to the
+ * resident blocks per SM (0: as many as fit); defer_after: attempts of one cell
+ * (over all its host steps) after which the persistent kernel hands it to the
  * warp-cooperative kernel (0: never, -1 keeps the current value). */
 int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after);
 

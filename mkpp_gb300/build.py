@@ -56,6 +56,9 @@ def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None 
     tmp = out.with_suffix(f".so.tmp{os.getpid()}")
     cmd = [
         nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+        # Only explicit fma() calls fuse: the unrolled and the warp-cooperative
+        # attempt then round identically, element by element.
+        "--fmad=false",
         "--extended-lambda", "-Xptxas", "-v" if verbose else "-O3",
         f"-DMKPP_MECH_HEADER=\"{mech}.cuh\"", f"-DMKPP_MECH_NS=mkpp_{mech}",
         f"-I{GEN}", f"-I{CSRC}", f"-I{INCLUDE}",

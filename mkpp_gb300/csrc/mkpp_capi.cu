@@ -90,15 +90,15 @@ constexpr size_t kQueueBytes = 256;
 //  register_variant  launch-bounds minimum of resident blocks (2: up to 255
 //                    registers per thread, 4: up to 128, more resident warps);
 //  blocks_per_sm     cap on resident blocks per SM (0: as many as fit);
-//  defer_after       attempts within one host step after which the persistent
-//                    kernel parks a cell for the warp-cooperative kernel
-//                    (0: never).
+//  defer_after       attempts of one cell (all host steps) after which the
+//                    persistent kernel parks it for the warp-cooperative
+//                    kernel (0: never).
 // Initial values come from MKPP_REGISTER_VARIANT, MKPP_BLOCKS_PER_SM and
 // MKPP_DEFER_AFTER, and mkpp_set_launch_tuning changes them.
 struct Tuning {
   int register_variant = 2;
   int blocks_per_sm = 0;
-  int defer_after = 2048;
+  int defer_after = 4096;
 };
 
 Tuning& tuning() {

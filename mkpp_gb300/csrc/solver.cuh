@@ -37,8 +37,8 @@ struct LaunchArgs {
   unsigned int* queue;       // persistent kernel work counter (zeroed before launch)
   const int* order;          // persistent kernel: queue position -> cell, or null (identity)
   // Hand-off of slow cells to the warp-cooperative kernel: a cell whose
-  // attempts within one host step reach defer_after (> 0) is parked in
-  // defer[] (controller state) with its state written back to conc.
+  // attempts (over all its host steps so far) reach defer_after (> 0) is
+  // parked in defer[] (controller state) with its state written back to conc.
   struct Deferred* defer;
   unsigned int* defer_count;
   int defer_after;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         if (!ctl.running()) {
           if (++step < a.steps) ctl.start(a.dt, a.seed);
           else done = true;
-        } else if (a.defer_after > 0 && ctl.attempts >= a.defer_after) {
+        } else if (a.defer_after > 0 && nacc + nrej >= a.defer_after) {
           // Too slow for one lane: park the cell for the cooperative kernel.
           const unsigned slot = atomicAdd(a.defer_count, 1u);
           Deferred d;
