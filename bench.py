@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--cpu-cells", type=int, default=256, help="cells in the bounded CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--max-attempts", type=int, default=100000)
+    ap.add_argument("--max-attempts", type=int, default=20000)
     ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous host step)")
     return ap.parse_args()
 
@@ -384,7 +384,7 @@ def main():
         ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
         ctx.set_aerosol(relative_humidity=rh_h.numpy())
         e2e_times = []
-        for rep in range(2):
+        for rep in range(1):
             work_conc.copy_(host_conc)
             barrier(world)
             t0 = time.perf_counter()

@@ -87,7 +87,8 @@ int mkpp_get_last_error(mkpp_handle_t handle, char* buffer, size_t buffer_len);
 /* ---- Handle options (no reference C entry; the reference exposes the
  * seed as the SolverKernels::initial_step_seed member, integrate.j2:42) --- */
 int mkpp_set_initial_step_seed(mkpp_handle_t handle, double seed);
-/* Upper bound on attempts per integrate() call (default 100000). */
+/* Upper bound on attempts per integrate() call (default 20000); a cell that
+ * reaches it reports MKPP_CELL_ERR_CONVERGENCE. */
 int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts);
 /* Read back the per-cell status / accepted / rejected counts of the last
  * mkpp_integrate (each array num_cells ints; any may be NULL). */

@@ -305,7 +305,7 @@ class DeviceSolver:
         self._check(rc)
         return ktab, status
 
-    def integrate_k(self, conc, ktab, dt, steps=1, seed=None, max_attempts=100000, mode="persistent",
+    def integrate_k(self, conc, ktab, dt, steps=1, seed=None, max_attempts=20000, mode="persistent",
                     status=None, accepted=None, rejected=None, order=None, k_step_stride=0):
         torch = self.torch
         ns, n = conc.shape
@@ -319,7 +319,7 @@ class DeviceSolver:
         self._check(rc)
 
     def integrate(self, conc, dt, steps=1, temp=None, rho=None, rh=None, clw=None, param=None, seed=None,
-                  max_attempts=100000, mode="persistent"):
+                  max_attempts=20000, mode="persistent"):
         """Integrate in place; returns (status, accepted, rejected) int32 tensors."""
         torch = self.torch
         n = conc.shape[1]
@@ -329,7 +329,7 @@ class DeviceSolver:
         self.integrate_k(conc, ktab, dt, steps, seed, max_attempts, mode, status, acc, rej)
         return status, acc, rej
 
-    def integrate_logged(self, conc, ktab, dt, steps=1, seed=None, max_attempts=100000, log_cap=4096):
+    def integrate_logged(self, conc, ktab, dt, steps=1, seed=None, max_attempts=20000, log_cap=4096):
         torch = self.torch
         n = conc.shape[1]
         if seed is None:

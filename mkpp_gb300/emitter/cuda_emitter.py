@@ -290,8 +290,8 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     _c_array(c, "int", "op_e", op_e)
     _c_array(c, "int", "op_kind", op_kind)
     _c_array(c, "int", "op_dg", op_dg)
-    _c_array(c, "int", "prod_l", prod_l)
-    _c_array(c, "int", "prod_r", prod_r)
+    c(f"static __device__ const int2 prod[{max(1, len(prod_l))}] = {{"
+      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(prod_l, prod_r)) + "};")
     c(f"constexpr int F_LEVELS = {nfl};")
     c(f"constexpr int B_LEVELS = {nbl};")
     _c_array(c, "int", "f_rows", f_rows)
@@ -299,11 +299,11 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     _c_array(c, "int", "b_rows", b_rows)
     _c_array(c, "int", "b_lev_off", b_lev_off)
     _c_array(c, "int", "lo_off", lo_off)
-    _c_array(c, "int", "lo_col", lo_col)
-    _c_array(c, "int", "lo_slot", lo_slot)
+    c(f"static __device__ const int2 lo[{max(1, len(lo_col))}] = {{"
+      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(lo_slot, lo_col)) + "};")
     _c_array(c, "int", "up_off", up_off)
-    _c_array(c, "int", "up_col", up_col)
-    _c_array(c, "int", "up_slot", up_slot)
+    c(f"static __device__ const int2 up[{max(1, len(up_col))}] = {{"
+      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(up_slot, up_col)) + "};")
     _c_array(c, "int", "diag", plan.diag)
     c("}  // namespace coop")
     c("")
@@ -340,7 +340,9 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {")
     c("        const int i = T::f_rows[j];")
     c("        double v = S[base + i];")
-    c("        for (int e = T::lo_off[i]; e < T::lo_off[i + 1]; ++e) v = fma(-S[T::lo_slot[e]], S[base + T::lo_col[e]], v);")
+    c("        const int e1 = T::lo_off[i + 1];")
+    c("        #pragma unroll 4")
+    c("        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }")
     c("        S[base + i] = v;")
     c("      }")
     c("      __syncwarp();")
@@ -349,7 +351,9 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {")
     c("        const int i = T::b_rows[j];")
     c("        double v = S[base + i];")
-    c("        for (int e = T::up_off[i]; e < T::up_off[i + 1]; ++e) v = fma(-S[T::up_slot[e]], S[base + T::up_col[e]], v);")
+    c("        const int e1 = T::up_off[i + 1];")
+    c("        #pragma unroll 4")
+    c("        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }")
     c("        S[base + i] = v * S[T::diag[i]];")
     c("      }")
     c("      __syncwarp();")
@@ -390,7 +394,9 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {")
     c("        const int out = T::op_out[j];")
     c("        double v = T::op_w[j] ? S[out] : 0.0;")
-    c("        for (int q = T::op_b[j]; q < T::op_e[j]; ++q) v = fma(-S[T::prod_l[q]], S[T::prod_r[q]], v);")
+    c("        const int q1 = T::op_e[j];")
+    c("        #pragma unroll 4")
+    c("        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }")
     c("        const int kind = T::op_kind[j];")
     c("        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }")
     c("        else if (kind == 2) S[out] = v * S[T::op_dg[j]];")

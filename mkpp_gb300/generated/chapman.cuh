@@ -30,8 +30,7 @@ static __device__ const int op_b[9] = {0, 0, 0, 0, 0, 0, 1, 2, 3};
 static __device__ const int op_e[9] = {0, 0, 0, 0, 0, 1, 2, 3, 5};
 static __device__ const int op_kind[9] = {1, 0, 0, 2, 2, 1, 0, 2, 1};
 static __device__ const int op_dg[9] = {0, 0, 0, 0, 0, 0, 0, 4, 0};
-static __device__ const int prod_l[5] = {3, 3, 6, 6, 7};
-static __device__ const int prod_r[5] = {1, 2, 1, 2, 5};
+static __device__ const int2 prod[5] = {{3, 1}, {3, 2}, {6, 1}, {6, 2}, {7, 5}};
 constexpr int F_LEVELS = 3;
 constexpr int B_LEVELS = 3;
 static __device__ const int f_rows[3] = {0, 1, 2};
@@ -39,11 +38,9 @@ static __device__ const int f_lev_off[4] = {0, 1, 2, 3};
 static __device__ const int b_rows[3] = {2, 1, 0};
 static __device__ const int b_lev_off[4] = {0, 1, 2, 3};
 static __device__ const int lo_off[4] = {0, 0, 1, 3};
-static __device__ const int lo_col[3] = {0, 0, 1};
-static __device__ const int lo_slot[3] = {3, 6, 7};
+static __device__ const int2 lo[3] = {{3, 0}, {6, 0}, {7, 1}};
 static __device__ const int up_off[4] = {0, 2, 3, 3};
-static __device__ const int up_col[3] = {1, 2, 2};
-static __device__ const int up_slot[3] = {1, 2, 5};
+static __device__ const int2 up[3] = {{1, 1}, {2, 2}, {5, 2}};
 static __device__ const int diag[3] = {0, 4, 8};
 }  // namespace coop
 
@@ -312,7 +309,9 @@ struct Mech {
       for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {
         const int i = T::f_rows[j];
         double v = S[base + i];
-        for (int e = T::lo_off[i]; e < T::lo_off[i + 1]; ++e) v = fma(-S[T::lo_slot[e]], S[base + T::lo_col[e]], v);
+        const int e1 = T::lo_off[i + 1];
+        #pragma unroll 4
+        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }
         S[base + i] = v;
       }
       __syncwarp();
@@ -321,7 +320,9 @@ struct Mech {
       for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {
         const int i = T::b_rows[j];
         double v = S[base + i];
-        for (int e = T::up_off[i]; e < T::up_off[i + 1]; ++e) v = fma(-S[T::up_slot[e]], S[base + T::up_col[e]], v);
+        const int e1 = T::up_off[i + 1];
+        #pragma unroll 4
+        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }
         S[base + i] = v * S[T::diag[i]];
       }
       __syncwarp();
@@ -362,7 +363,9 @@ struct Mech {
       for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {
         const int out = T::op_out[j];
         double v = T::op_w[j] ? S[out] : 0.0;
-        for (int q = T::op_b[j]; q < T::op_e[j]; ++q) v = fma(-S[T::prod_l[q]], S[T::prod_r[q]], v);
+        const int q1 = T::op_e[j];
+        #pragma unroll 4
+        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }
         const int kind = T::op_kind[j];
         if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }
         else if (kind == 2) S[out] = v * S[T::op_dg[j]];

@@ -30,8 +30,7 @@ static __device__ const int op_b[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 0
 static __device__ const int op_e[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 1, 2, 5, 4, 6, 7, 8, 11, 14, 12, 16, 18, 23, 20, 25, 29};
 static __device__ const int op_kind[29] = {1, 0, 1, 0, 0, 0, 2, 2, 2, 2, 2, 2, 2, 0, 1, 0, 0, 2, 2, 2, 1, 0, 0, 2, 2, 0, 1, 2, 1};
 static __device__ const int op_dg[29] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 3, 3, 3, 3, 0, 0, 0, 0, 9, 9, 9, 0, 0, 0, 16, 16, 0, 0, 22, 0};
-static __device__ const int prod_l[29] = {2, 8, 7, 8, 8, 14, 19, 24, 13, 14, 15, 15, 14, 15, 19, 20, 24, 25, 20, 21, 19, 20, 21, 25, 26, 24, 25, 26, 27};
-static __device__ const int prod_r[29] = {1, 4, 1, 5, 6, 4, 4, 4, 1, 5, 10, 11, 6, 12, 5, 10, 5, 10, 11, 17, 6, 12, 18, 11, 17, 6, 12, 18, 23};
+static __device__ const int2 prod[29] = {{2, 1}, {8, 4}, {7, 1}, {8, 5}, {8, 6}, {14, 4}, {19, 4}, {24, 4}, {13, 1}, {14, 5}, {15, 10}, {15, 11}, {14, 6}, {15, 12}, {19, 5}, {20, 10}, {24, 5}, {25, 10}, {20, 11}, {21, 17}, {19, 6}, {20, 12}, {21, 18}, {25, 11}, {26, 17}, {24, 6}, {25, 12}, {26, 18}, {27, 23}};
 constexpr int F_LEVELS = 6;
 constexpr int B_LEVELS = 5;
 static __device__ const int f_rows[6] = {0, 1, 2, 3, 4, 5};
@@ -39,11 +38,9 @@ static __device__ const int f_lev_off[7] = {0, 1, 2, 3, 4, 5, 6};
 static __device__ const int b_rows[6] = {5, 4, 3, 0, 2, 1};
 static __device__ const int b_lev_off[6] = {0, 1, 2, 3, 5, 6};
 static __device__ const int lo_off[7] = {0, 0, 1, 3, 6, 9, 13};
-static __device__ const int lo_col[13] = {0, 0, 1, 0, 1, 2, 1, 2, 3, 1, 2, 3, 4};
-static __device__ const int lo_slot[13] = {2, 7, 8, 13, 14, 15, 19, 20, 21, 24, 25, 26, 27};
+static __device__ const int2 lo[13] = {{2, 0}, {7, 0}, {8, 1}, {13, 0}, {14, 1}, {15, 2}, {19, 1}, {20, 2}, {21, 3}, {24, 1}, {25, 2}, {26, 3}, {27, 4}};
 static __device__ const int up_off[7] = {0, 1, 4, 7, 9, 10, 10};
-static __device__ const int up_col[10] = {3, 2, 3, 5, 3, 4, 5, 4, 5, 5};
-static __device__ const int up_slot[10] = {1, 4, 5, 6, 10, 11, 12, 17, 18, 23};
+static __device__ const int2 up[10] = {{1, 3}, {4, 2}, {5, 3}, {6, 5}, {10, 3}, {11, 4}, {12, 5}, {17, 4}, {18, 5}, {23, 5}};
 static __device__ const int diag[6] = {0, 3, 9, 16, 22, 28};
 }  // namespace coop
 
@@ -465,7 +462,9 @@ struct Mech {
       for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {
         const int i = T::f_rows[j];
         double v = S[base + i];
-        for (int e = T::lo_off[i]; e < T::lo_off[i + 1]; ++e) v = fma(-S[T::lo_slot[e]], S[base + T::lo_col[e]], v);
+        const int e1 = T::lo_off[i + 1];
+        #pragma unroll 4
+        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }
         S[base + i] = v;
       }
       __syncwarp();
@@ -474,7 +473,9 @@ struct Mech {
       for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {
         const int i = T::b_rows[j];
         double v = S[base + i];
-        for (int e = T::up_off[i]; e < T::up_off[i + 1]; ++e) v = fma(-S[T::up_slot[e]], S[base + T::up_col[e]], v);
+        const int e1 = T::up_off[i + 1];
+        #pragma unroll 4
+        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }
         S[base + i] = v * S[T::diag[i]];
       }
       __syncwarp();
@@ -515,7 +516,9 @@ struct Mech {
       for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {
         const int out = T::op_out[j];
         double v = T::op_w[j] ? S[out] : 0.0;
-        for (int q = T::op_b[j]; q < T::op_e[j]; ++q) v = fma(-S[T::prod_l[q]], S[T::prod_r[q]], v);
+        const int q1 = T::op_e[j];
+        #pragma unroll 4
+        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }
         const int kind = T::op_kind[j];
         if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }
         else if (kind == 2) S[out] = v * S[T::op_dg[j]];

@@ -210,7 +210,7 @@ class Oracle:
         return k, dk
 
     def integrate(self, conc, dt, steps=1, temp=None, rho=None, rh=None, clw=None, param=None,
-                  seed=None, max_attempts=100000, nthreads=0, log_cap=0, replay=None, k=None, dk=None):
+                  seed=None, max_attempts=20000, nthreads=0, log_cap=0, replay=None, k=None, dk=None):
         """Integrate in place a (species x cells) array; returns a dict of diagnostics."""
         conc = np.ascontiguousarray(conc, dtype=np.float64)
         ns, n = conc.shape
