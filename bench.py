@@ -41,6 +41,14 @@ METRIC = "SAPRC99 cell-solves/s on 1 GB300 at rtol 1e-3"
 UNIT = "cell-solves/s"
 
 
+T_START = time.time()
+
+
+def log(msg):
+    """Progress on stderr (the JSON result line is the only stdout output)."""
+    print(f"[bench {time.time() - T_START:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -54,7 +62,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--max-attempts", type=int, default=20000)
-    ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous host step)")
+    ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous window)")
+    ap.add_argument("--forms-cells", type=int, default=65536, help="cells of the plain-vs-persistent comparison")
+    ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
     return ap.parse_args()
 
 
@@ -284,6 +294,7 @@ def main():
             window(ev)
             stream.synchronize()
             kernel_ms.append(ev[0].elapsed_time(ev[1]))
+            log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms")
     # Capture the window (hs rate-constant launches + 1 integrate launch).
     g = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
@@ -301,6 +312,7 @@ def main():
         torch.cuda.synchronize()
     barrier(world)
     el_ms = max_over_ranks(start.elapsed_time(end), world) / args.steps
+    log(f"timed: {el_ms:.0f} ms per window")
     clk = clocks.summary()
     cell_solves = n * hs * world
     value = cell_solves / (el_ms * 1e-3)
@@ -337,8 +349,10 @@ def main():
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
         "gpu_launches": args.steps * (hs + 1),
-        "launch": {"min_blocks": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
-                   "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"), "cost_order": bool(args.order)},
+        "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
+                   "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
+                   "defer_after": os.environ.get("MKPP_DEFER_AFTER", "4096"), "cost_order": bool(args.order),
+                   "max_attempts_per_call": args.max_attempts},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
                  "attempts_per_cell_window_pct": {q: float(np.percentile(att, q)) for q in (50, 90, 99, 100)},
@@ -355,22 +369,41 @@ def main():
     }
 
     if rank == 0 and not args.no_plain:
-        # Plain form: one launch per host step, one thread per cell, no queue.
-        pe = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        with torch.cuda.stream(stream):
-            pe[0].record(stream)
-            conc.copy_(conc0)
-            rates()
-            for s in range(hs):
-                check(lib.mkpp_gpu_integrate_k(C.c_size_t(n), p(conc), p(ktab[s]), C.c_size_t(0), 1,
-                                               C.c_double(w.dt), C.c_double(seed), args.max_attempts, 0, None,
-                                               p(status), p(acc), p(rej), p(ws), C.c_size_t(ws.numel()), sp),
-                      "integrate plain")
-            pe[1].record(stream)
-            stream.synchronize()
-        pm = pe[0].elapsed_time(pe[1])
-        result["plain_form"] = {"value": n * hs / (pm * 1e-3), "unit": UNIT, "ms_per_step": pm,
-                                "form": f"one thread per cell, one launch per host step ({2 * hs} eager launches)"}
+        # Forms on a sub-configuration (first forms_cells cells, first
+        # forms_host_steps host steps): plain = one launch per host step, one
+        # thread per cell, no queue; persistent = the window form above.
+        fn, fh = min(n, args.forms_cells), min(hs, args.forms_host_steps)
+        sub = conc0[:, :fn].contiguous()
+        c2 = sub.clone()
+        k2 = ktab[:fh, :, :fn].contiguous()
+        s2, a2, r2 = status[:fn].clone(), acc[:fn].clone(), rej[:fn].clone()
+        res = {}
+        for form in ("plain", "persistent"):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                c2.copy_(sub)
+                s2.zero_()
+                e0.record(stream)
+                if form == "plain":
+                    for s in range(fh):
+                        check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2[s]), C.c_size_t(0), 1,
+                                                       C.c_double(w.dt), C.c_double(seed), args.max_attempts, 0,
+                                                       None, p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
+                              "integrate plain")
+                else:
+                    check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2), C.c_size_t(NR * fn), fh,
+                                                   C.c_double(w.dt), C.c_double(seed), args.max_attempts, 1, None,
+                                                   p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
+                          "integrate persistent")
+                e1.record(stream)
+                stream.synchronize()
+            ms = e0.elapsed_time(e1)
+            res[form] = {"value": fn * fh / (ms * 1e-3), "ms": ms}
+            log(f"form {form}: {ms:.0f} ms")
+        result["forms"] = {"config": f"first {fn} cells x {fh} host steps", "unit": UNIT,
+                           "plain": dict(res["plain"], form="one thread per cell, one launch per host step"),
+                           "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
+                                                                     "one launch for all host steps")}
 
     if not args.no_e2e:
         # End to end through the reference-facing host C ABI with pinned host buffers.
@@ -393,6 +426,7 @@ def main():
                 ctx.integrate(w.dt)
             e2e_times.append(time.perf_counter() - t0)
         e2e_s = max_over_ranks(min(e2e_times), world)
+        log(f"e2e: {e2e_s:.1f} s")
         h2d = hs * n * 8 * (NS + 3 + NP)
         d2h = hs * n * 8 * NS
         result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -402,6 +436,7 @@ def main():
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
         kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
+        log(f"cpu baseline ({kind}): {el:.1f} s")
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                                   "sample": f"first {args.cpu_cells} of {n} cells x {hs} host steps of {w.dt:g} s",
                                   "seconds": el}

@@ -206,6 +206,16 @@ __device__ __forceinline__ bool state_finite(SA& S) {
   return ok;
 }
 
+// Rate constants of host step `step` of cell c into the working storage, so
+// that every attempt reads them from the cell's own slots.
+template <class Mech, class SA>
+__device__ __forceinline__ void load_rates(const LaunchArgs& a, size_t c, int step, SA& S) {
+  const double* __restrict__ k = a.ktab + (size_t)step * a.k_step_stride + c;
+  const size_t n = (size_t)a.ncells;
+#pragma unroll 8
+  for (int r = 0; r < Mech::NR; ++r) S[Mech::KT + r] = __ldg(k + (size_t)r * n);
+}
+
 template <class Mech, class SA>
 __device__ __forceinline__ void apply_increment(SA& S) {
 #pragma unroll
@@ -232,7 +242,8 @@ __device__ __forceinline__ int integrate_cell(SA& S, const LaunchArgs& a, size_t
   bool capped = false, zero_pivot = false;
   nacc = nrej = 0;
   for (int step = 0; step < a.steps && !capped; ++step) {
-    const KTable k{a.ktab + (size_t)step * a.k_step_stride + c, n};
+    load_rates<Mech>(a, c, step, S);
+    auto k = [&](int r) { return S[Mech::KT + r]; };
     Controller ctl;
     ctl.start(a.dt, a.seed);
     while (ctl.running()) {
@@ -323,7 +334,10 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           step = 0;
           nacc = nrej = 0;
           capped = zero_pivot = false;
-          if (!flagged) load_state<Mech>(a.conc, (size_t)cell, n, S);
+          if (!flagged) {
+            load_state<Mech>(a.conc, (size_t)cell, n, S);
+            load_rates<Mech>(a, (size_t)cell, 0, S);
+          }
           ctl.start(a.dt, a.seed);
         }
       }
@@ -337,7 +351,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         capped = true;
         done = true;
       } else {
-        const KTable k{a.ktab + (size_t)step * a.k_step_stride + cell, n};
+        auto k = [&](int r) { return S[Mech::KT + r]; };
         const double h = ctl.next_h();
         int st = 0;
         const double err = Mech::attempt(S, k, h, st);
@@ -349,8 +363,12 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           ++nrej;
         }
         if (!ctl.running()) {
-          if (++step < a.steps) ctl.start(a.dt, a.seed);
-          else done = true;
+          if (++step < a.steps) {
+            ctl.start(a.dt, a.seed);
+            load_rates<Mech>(a, (size_t)cell, step, S);
+          } else {
+            done = true;
+          }
         } else if (a.defer_after > 0 && nacc + nrej >= a.defer_after) {
           // Too slow for one lane: park the cell for the cooperative kernel.
           const unsigned slot = atomicAdd(a.defer_count, 1u);
@@ -415,7 +433,9 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
     bool zero_pivot = (d.flags & 4) != 0, capped = false;
     int nacc = d.nacc, nrej = d.nrej;
     for (int step = d.step; step < a.steps;) {
-      const KTable k{a.ktab + (size_t)step * a.k_step_stride + c, n};
+      for (int r = lane; r < Mech::NR; r += 32) S[Mech::KT + r] = a.ktab[(size_t)step * a.k_step_stride + c + n * r];
+      __syncwarp();
+      auto k = [&](int r) { return S[Mech::KT + r]; };
       while (ctl.running()) {
         if (ctl.attempts >= a.max_attempts) {
           capped = true;

@@ -571,13 +571,16 @@ def emit_mechanism(plan: ReducedPlan) -> str:
     K0 = Y + nv
     FS = K0 + stages * nv
     DY = FS + nv
-    nslots = DY + nv
+    KT = DY + nv
+    nslots = KT + nr
     c("  // Per-cell working storage, in slots of one double: the LU factors, the")
-    c("  // state y, the stage vectors K_1..K_s, the tendency F and the increment dy.")
+    c("  // state y, the stage vectors K_1..K_s, the tendency F, the increment dy and")
+    c("  // the rate constants of the current host step.")
     c(f"  static constexpr int Y = {Y};")
     c(f"  static constexpr int K0 = {K0};")
     c(f"  static constexpr int F = {FS};")
     c(f"  static constexpr int DY = {DY};")
+    c(f"  static constexpr int KT = {KT};        // the cell's rate constants for the current host step")
     c(f"  static constexpr int NSLOTS = {nslots};")
     c("")
     # ---------------- Fun

@@ -99,12 +99,14 @@ struct Mech {
   }
 
   // Per-cell working storage, in slots of one double: the LU factors, the
-  // state y, the stage vectors K_1..K_s, the tendency F and the increment dy.
+  // state y, the stage vectors K_1..K_s, the tendency F, the increment dy and
+  // the rate constants of the current host step.
   static constexpr int Y = 29;
   static constexpr int K0 = 35;
   static constexpr int F = 53;
   static constexpr int DY = 59;
-  static constexpr int NSLOTS = 65;
+  static constexpr int KT = 65;        // the cell's rate constants for the current host step
+  static constexpr int NSLOTS = 75;
 
   // Mass-action tendencies F(y) of the variable species (logical order):
   // y(i) supplies the state, out(i, F_i) receives the result.
