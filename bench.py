@@ -351,7 +351,7 @@ def main():
         "gpu_launches": args.steps * (hs + 1),
         "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
-                   "defer_after": os.environ.get("MKPP_DEFER_AFTER", "4096"), "cost_order": bool(args.order),
+                   "defer_after": os.environ.get("MKPP_DEFER_AFTER", "0"), "cost_order": bool(args.order),
                    "max_attempts_per_call": args.max_attempts},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],

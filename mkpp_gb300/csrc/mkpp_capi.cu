@@ -96,13 +96,16 @@ constexpr size_t kQueueBytes = 256;
 //  blocks_per_sm     cap on resident blocks per SM (0: as many as fit);
 //  defer_after       attempts of one cell (all host steps) after which the
 //                    persistent kernel parks it for the warp-cooperative
-//                    kernel (0: never).
+//                    kernel (0: never, the default).  On GB300 a warp FP64
+//                    instruction costs the same pipe time with one active lane
+//                    as with 32, and the sparse LU keeps few lanes busy, so
+//                    the cooperative form does not beat one lane per cell.
 // Initial values come from MKPP_REGISTER_VARIANT, MKPP_BLOCKS_PER_SM and
 // MKPP_DEFER_AFTER, and mkpp_set_launch_tuning changes them.
 struct Tuning {
   int register_variant = 2;
   int blocks_per_sm = 0;
-  int defer_after = 4096;
+  int defer_after = 0;
 };
 
 Tuning& tuning() {

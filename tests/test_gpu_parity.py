@@ -280,6 +280,6 @@ def test_cooperative_handoff_is_bit_identical(built_libs, mech, defer_after):
             torch.cuda.synchronize()
             outs.append((conc.cpu().numpy(), st.cpu().numpy(), acc.cpu().numpy(), rej.cpu().numpy()))
     finally:
-        s.set_tuning(defer_after=4096)
+        s.set_tuning(defer_after=0)
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b, equal_nan=True)
