@@ -161,6 +161,28 @@ int mkpp_gpu_evaluate_rates(size_t num_cells, const double* conc, const double* 
 int mkpp_gpu_evaluate_jacobian(size_t num_cells, const double* conc, const double* ktab,
                                double* jac_out, void* stream);
 
+/* Allocation-free integrate (no counterpart in the reference).  For callers
+ * that cannot allocate device memory at the point where they integrate: a
+ * host model that records its time step into a CUDA graph (cudaMalloc is not
+ * allowed while a stream is being captured), or one whose memory pool owns
+ * all free device memory.  Same semantics as mkpp_gpu_integrate_k in plain
+ * mode (one thread per cell), but the LU and stage scratch is a static
+ * device array inside the library, sized for MKPP_NOALLOC_MAX_CELLS cells
+ * (for SAPRC99 1024 x 2226 doubles, 18 MB), which every GPU that loads the
+ * library holds until the process exits.  Larger num_cells is rejected with
+ * MKPP_ERROR_INVALID_ARGUMENT and a message on stderr.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must not be issued.  Nothing in the array
+ * needs clearing between calls; each cell's slots are written before they
+ * are read.  Makes no cudaMalloc or cudaFree call. */
+#define MKPP_NOALLOC_MAX_CELLS 1024
+int mkpp_gpu_integrate_noalloc(size_t num_cells, double* conc, const double* ktab,
+                               size_t k_step_stride, int steps, double dt, double seed,
+                               int max_attempts, int* status, int* accepted, int* rejected,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,6 +80,7 @@ SIGNATURES = [
                                        _vp]),
     ("mkpp_gpu_evaluate_rates", _i, [_sz, _vp, _vp, _vp, _vp]),
     ("mkpp_gpu_evaluate_jacobian", _i, [_sz, _vp, _vp, _vp, _vp]),
+    ("mkpp_gpu_integrate_noalloc", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _vp, _vp, _vp, _vp]),
 ]
 
 _LIBS: dict[str, C.CDLL] = {}

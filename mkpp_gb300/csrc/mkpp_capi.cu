@@ -15,6 +15,8 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "../../include/mkpp.h"
@@ -296,7 +298,70 @@ __global__ void __launch_bounds__(128, 1) mkpp_fixed_columns_kernel(size_t n, co
   }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free integrate (mkpp_gpu_integrate_noalloc).
+//
+// Its LU/stage scratch is this file-scope device array instead of a
+// caller-provided workspace.  The array holds the working storage of
+// MKPP_NOALLOC_MAX_CELLS cells, laid out as the plain kernel's per-block
+// tiles (ceil(cells / 128) blocks of 128 threads).  Every GPU that loads the
+// library keeps it allocated until the process exits.  In host code the
+// name g_noalloc_scratch is only a host-side stand-in; the device address is
+// obtained once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxCells = MKPP_NOALLOC_MAX_CELLS;
+constexpr size_t kNoAllocDoubles = StoreInfo::kTile ? (size_t)kNoAllocMaxCells * Mech::NSLOTS : 1;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, set up on the
+// first call made with that device current.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MKPP_ERROR_DEVICE;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    double* ptr = nullptr;
+    if (cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return MKPP_ERROR_DEVICE;
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MKPP_SUCCESS;
+}
+
 }  // namespace
+
+extern "C" {
+
+int mkpp_gpu_integrate_noalloc(size_t num_cells, double* conc, const double* ktab, size_t k_step_stride,
+                               int steps, double dt, double seed, int max_attempts, int* status, int* accepted,
+                               int* rejected, void* stream) {
+  if (!conc || !ktab) return MKPP_ERROR_NULL_POINTER;
+  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (num_cells > (size_t)kNoAllocMaxCells) {
+    std::fprintf(stderr,
+                 "FATAL ERROR: mkpp_gpu_integrate_noalloc: %zu cells exceed its static scratch capacity of %d "
+                 "cells; split the call or use mkpp_gpu_integrate_k with a workspace\n",
+                 num_cells, kNoAllocMaxCells);
+    return MKPP_ERROR_INVALID_ARGUMENT;
+  }
+  if (!std::isfinite(dt) || dt <= 0.0 || steps < 1 || !(seed > 0.0) || max_attempts < 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (k_step_stride != 0 && k_step_stride < num_cells * Mech::NR) return MKPP_ERROR_INVALID_ARGUMENT;
+  double* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc != MKPP_SUCCESS) return rc;
+  mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
+  a.k_step_stride = k_step_stride;
+  const int grid = (int)((num_cells + mkpp::kBlock - 1) / mkpp::kBlock);
+  mkpp::integrate_plain_kernel<Mech, 2><<<grid, mkpp::kBlock, 0, (cudaStream_t)stream>>>(
+      a, StoreInfo::kTile ? scratch : nullptr);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+}  // extern "C"
 
 extern "C" {
 
