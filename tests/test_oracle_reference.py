@@ -1,0 +1,96 @@
+"""The oracle against the reference's own generated CPU solver.
+
+``oracle/ref_build.py`` regenerates the reference's Kokkos headers with the
+reference's compiler and compiles them, unmodified, behind a small driver.
+These tests compare the oracle port with that build on seeded inputs:
+
+* tendencies (``compute_rates``) and the dense Jacobian (``compute_jacobian``,
+  src/mkpp/templates/kernels.j2) to round-off, which pins the rate constants,
+  the flux products and the Jacobian pattern of every reaction;
+* ``SolverKernels<D>::integrate()`` (src/mkpp/templates/integrate.j2) over one
+  host step.  Chapman and the stratospheric mechanism agree to round-off.
+  SAPRC99 as shipped has rate constants up to 1e37 (reactions 11, 32, 69),
+  where a one-ulp difference in k moves the solution by 1e-6 and can change
+  the accepted step sequence.  There the bound is statistical, the same two
+  bounds the GPU parity tests use for the shipped rates: median to
+  round-off, every cell within 1e-2.
+
+Skipped when the reference build is absent (no reference checkout and no
+previously generated headers).
+"""
+
+import numpy as np
+import pytest
+
+from mkpp_gb300 import workloads
+from oracle import ref_build
+from oracle.oracle import Oracle
+
+
+def _ref(mech):
+    try:
+        ref_build.build_if_available()
+    except Exception as e:  # pragma: no cover - toolchain problems surface as skips
+        pytest.skip(f"reference build failed: {e}")
+    solver = ref_build.load(mech)
+    if solver is None:
+        pytest.skip("reference solver library not built")
+    return solver
+
+
+@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99"])
+def test_tendencies_and_jacobian_match_reference(mech):
+    ref = _ref(mech)
+    o = Oracle(mech)
+    w = workloads.make(mech, 64)
+    for step in (0, 3):
+        P = w.param_at(step)
+        F0, J0 = ref.evaluate(w.conc, w.temp, w.rho, w.rh, P)
+        F1, Jc = o.evaluate(w.conc, w.temp, w.rho, w.rh, param=P)
+        J1 = o.dense_jacobian(Jc)
+        scale = np.maximum(np.abs(F0).max(axis=0, keepdims=True), 1e-300)
+        assert (np.abs(F1 - F0) / scale).max() < 1e-13
+        pattern = np.zeros(J0.shape[:2], bool)
+        for i, j in o.raw["jacobian_entries"]:
+            pattern[i, j] = True
+        # The reference writes nothing outside the exported sparsity pattern.
+        assert not np.any(J0[~pattern])
+        nz = J0 != 0
+        assert (np.abs(J1 - J0)[nz] / np.abs(J0[nz])).max() < 1e-11
+        assert not np.any(J1[~nz])
+
+
+@pytest.mark.parametrize("mech", ["chapman", "small_strato"])
+def test_integrate_matches_reference(mech):
+    ref = _ref(mech)
+    o = Oracle(mech)
+    w = workloads.make(mech, 128)
+    a, b = w.conc.copy(), w.conc.copy()
+    P = w.param_at(0)
+    ro = o.integrate(a, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
+    rr = ref.integrate(b, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
+    assert np.all(ro["status"] == 0)
+    rel = np.abs(ro["conc"] - rr["conc"]) / np.maximum(np.abs(rr["conc"]), 1.0)
+    assert rel.max() < 1e-12
+
+
+def test_integrate_matches_reference_saprc99_statistically():
+    ref = _ref("saprc99")
+    o = Oracle("saprc99")
+    w = workloads.make("saprc99", 64)
+    a, b = w.conc.copy(), w.conc.copy()
+    P = w.param_at(0)
+    ro = o.integrate(a, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
+    rr = ref.integrate(b, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
+    both = (ro["status"] == 0) & np.isfinite(rr["conc"]).all(axis=0)
+    assert both.mean() > 0.9
+    rel = np.abs(ro["conc"] - rr["conc"]) / np.maximum(np.abs(rr["conc"]), 1.0)
+    # Seeded sample (64 cells): element median 1e-13, a quarter of the cells
+    # to round-off, the worst cell 5e-3.
+    assert np.median(rel[:, both]) < 1e-11
+    per_cell = rel[:, both].max(axis=0)
+    assert np.quantile(per_cell, 0.25) < 1e-11
+    assert per_cell.max() < 1e-2
+    # A cell the reference leaves non-finite is one the port flags.
+    bad_ref = ~np.isfinite(rr["conc"]).all(axis=0)
+    assert np.all(ro["status"][bad_ref] != 0)
