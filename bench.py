@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous window)")
     ap.add_argument("--forms-cells", type=int, default=65536, help="cells of the plain-vs-persistent comparison")
     ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
+    ap.add_argument("--adjoint-cells", type=int, default=65536, help="cells of the adjoint/forward measurement")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -169,8 +171,6 @@ def cpu_reference_sample(w, cells: int, host_steps: int, threads: int):
     for s in range(host_steps):
         runner.integrate(conc, sub.dt, temp=sub.temp, rho=sub.rho, rh=sub.rh, param=sub.param_at(s),
                          nthreads=threads)
-        if kind == "port":
-            pass
     el = time.perf_counter() - t0
     return kind, cells * host_steps / el, el
 
@@ -404,6 +404,54 @@ def main():
                            "plain": dict(res["plain"], form="one thread per cell, one launch per host step"),
                            "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
                                                                      "one launch for all host steps")}
+
+    if rank == 0 and not args.no_adjoint:
+        # Discrete adjoint (SAPRC99 adjoint configuration): first adjoint_cells
+        # cells, one 3600 s integrate() with checkpoints at accepted steps, loss
+        # sum_c (O3_c - O3t_c)^2 with O3t log-normal (sigma 0.2) around the
+        # forward result; gradients w.r.t. all initial concentrations and all
+        # rate constants.  Reported: adjoint time / checkpointed-forward time.
+        from mkpp_gb300.adjoint import Checkpoints
+
+        na = min(n, args.adjoint_cells)
+        ca0 = conc0[:, :na].contiguous()
+        ka = ktab[0, :, :na].contiguous()
+        del ktab
+        torch.cuda.empty_cache()
+        cap = 1536
+        ck = Checkpoints(w.mechanism, na, cap, dev)
+        ev_f = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev_a = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ca = ca0.clone()
+        with torch.cuda.stream(stream):
+            ev_f[0].record(stream)
+            ck.forward(ca, ka, 3600.0, seed, args.max_attempts)
+            ev_f[1].record(stream)
+            stream.synchronize()
+            o3 = raw["species"].index("O3")
+            rng = torch.Generator(device="cpu").manual_seed(2718)
+            target = ca[o3] * torch.exp(0.2 * torch.randn(na, generator=rng, dtype=f64)).to(dev)
+            lam = torch.zeros_like(ca)
+            lam[o3] = 2.0 * (ca[o3] - target)
+            ev_a[0].record(stream)
+            gc, gk = ck.adjoint(ka, lam)
+            ev_a[1].record(stream)
+            stream.synchronize()
+        fms, ams = ev_f[0].elapsed_time(ev_f[1]), ev_a[0].elapsed_time(ev_a[1])
+        cnt = ck.count.cpu().numpy()
+        sts = ck.status.cpu().numpy()
+        result["adjoint"] = {
+            "config": f"first {na} cells, one 3600 s integrate(), loss sum (O3 - O3t)^2, O3t log-normal sigma 0.2",
+            "forward_checkpointed_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
+            "accepted_steps_pct": {q: float(np.percentile(cnt, q)) for q in (50, 99, 100)},
+            "checkpoint_cap": cap, "cell_status_counts": np.bincount(sts, minlength=6).tolist(),
+            "gradients": f"dL/dC0 for all species (fixed species 0) and dL/dk for all {len(raw['reactions'])} "
+                         "reactions, FP64",
+            "finite_gradients_frac": float(torch.isfinite(gc).all(0).double().mean()),
+        }
+        log(f"adjoint: forward {fms:.0f} ms, adjoint {ams:.0f} ms, ratio {ams / fms:.2f}")
+        del ck, gc, gk
+        torch.cuda.empty_cache()
 
     if not args.no_e2e:
         # End to end through the reference-facing host C ABI with pinned host buffers.

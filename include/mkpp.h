@@ -161,6 +161,37 @@ int mkpp_gpu_evaluate_rates(size_t num_cells, const double* conc, const double* 
 int mkpp_gpu_evaluate_jacobian(size_t num_cells, const double* conc, const double* ktab,
                                double* jac_out, void* stream);
 
+/* ---- Differentiation (discrete adjoint; the reference's counterparts are
+ * SolverKernels::integrate_fwd_checkpoint / integrate_adj,
+ * src/mkpp/templates/solver_variants/integrate_fwd_checkpoint.j2:36-295 and
+ * integrate_adj.j2:49-156, a frozen-Jacobian reverse sweep; this one is the
+ * full discrete adjoint of the accepted steps, with the Jacobian's
+ * dependence on the state and on the rate constants) ------------------- */
+#define MKPP_CELL_ERR_CHECKPOINT_OVERFLOW 5
+/* Workspace of the three calls below (per-thread scratch, 256-byte aligned). */
+size_t mkpp_gpu_adjoint_workspace_bytes(size_t num_cells);
+/* One integrate() call over dt (same controller and arithmetic as the plain
+ * form) that records, at every accepted step s < ckpt_cap, the state before
+ * the step at ckpt_y[(s * NV + i) * num_cells + cell] (NV variable species in
+ * the solver's order) and the step size at ckpt_h[s * num_cells + cell];
+ * ckpt_n[cell] = accepted steps.  More accepted steps than ckpt_cap:
+ * MKPP_CELL_ERR_CHECKPOINT_OVERFLOW. */
+int mkpp_gpu_integrate_checkpoint(size_t num_cells, double* conc, const double* ktab, double dt,
+                                  double seed, int max_attempts, int ckpt_cap, double* ckpt_y,
+                                  double* ckpt_h, int* ckpt_n, int* status, int* accepted,
+                                  int* rejected, void* workspace, size_t workspace_bytes, void* stream);
+/* Applies the recorded step sizes (frozen step sequence) to conc. */
+int mkpp_gpu_integrate_replay(size_t num_cells, double* conc, const double* ktab, int ckpt_cap,
+                              const double* ckpt_h, const int* ckpt_n, void* workspace,
+                              size_t workspace_bytes, void* stream);
+/* Given lambda_end = dL/dconc at the end of the checkpointed call
+ * ([species][cells]), writes dL/dconc at its start (fixed species 0) and
+ * dL/dk ([reactions][cells]) for the recorded step sequence. */
+int mkpp_gpu_adjoint(size_t num_cells, const double* ktab, int ckpt_cap, const double* ckpt_y,
+                     const double* ckpt_h, const int* ckpt_n, const double* lambda_end,
+                     double* grad_conc0, double* grad_k, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
 /* Allocation-free integrate (no counterpart in the reference).  For callers
  * that cannot allocate device memory at the point where they integrate: a
  * host model that records its time step into a CUDA graph (cudaMalloc is not

@@ -36,7 +36,7 @@ ERRORS = {
     -107: "MKPP_ERROR_DEVICE",
 }
 CELL_STATUS = {0: "SUCCESS", 1: "ERR_SINGULAR_MATRIX", 2: "ERR_NON_FINITE_STATE",
-               3: "ERR_CONVERGENCE_FAILURE", 4: "ERR_NUMERICAL_FAILURE"}
+               3: "ERR_CONVERGENCE_FAILURE", 4: "ERR_NUMERICAL_FAILURE", 5: "ERR_CHECKPOINT_OVERFLOW"}
 MODES = {"plain": 0, "persistent": 1}
 
 
@@ -80,6 +80,11 @@ SIGNATURES = [
                                        _vp]),
     ("mkpp_gpu_evaluate_rates", _i, [_sz, _vp, _vp, _vp, _vp]),
     ("mkpp_gpu_evaluate_jacobian", _i, [_sz, _vp, _vp, _vp, _vp]),
+    ("mkpp_gpu_adjoint_workspace_bytes", _sz, [_sz]),
+    ("mkpp_gpu_integrate_checkpoint", _i, [_sz, _vp, _vp, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
+                                           _vp]),
+    ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
+    ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_integrate_noalloc", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _vp, _vp, _vp, _vp]),
 ]
 

@@ -37,8 +37,15 @@ def lib_path(mech: str) -> Path:
     return LIB / f"libmkpp_{mech}.so"
 
 
+# One translation unit per large kernel instantiation, compiled in parallel:
+# the unrolled attempt of a large mechanism takes one to two minutes of
+# cicc + ptxas per kernel.  The heaviest units come first.
+UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_capi.cu", "mkpp_plain.cu",
+         "mkpp_persist4.cu", "mkpp_eval.cu", "mkpp_coop.cu", "mkpp_diff.cu")
+
+
 def _sources(mech: str) -> list[Path]:
-    return [CSRC / "mkpp_capi.cu", CSRC / "solver.cuh", CSRC / "mkpp_device.cuh",
+    return [*(CSRC / u for u in UNITS), CSRC / "capi_common.cuh", CSRC / "solver.cuh", CSRC / "mkpp_device.cuh",
             GEN / f"{mech}.cuh", INCLUDE / "mkpp.h", Path(__file__)]
 
 
@@ -50,29 +57,51 @@ def _stale(mech: str) -> bool:
     return any(s.exists() and s.stat().st_mtime > t for s in _sources(mech))
 
 
-def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None = None) -> Path:
-    out = lib_path(mech)
-    LIB.mkdir(parents=True, exist_ok=True)
-    tmp = out.with_suffix(f".so.tmp{os.getpid()}")
-    cmd = [
-        nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+def _flags(mech: str, verbose: bool) -> list[str]:
+    return [
+        *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
         # Only explicit fma() calls fuse: the unrolled and the warp-cooperative
         # attempt then round identically, element by element.
         "--fmad=false",
         "--extended-lambda", "-Xptxas", "-v" if verbose else "-O3",
         f"-DMKPP_MECH_HEADER=\"{mech}.cuh\"", f"-DMKPP_MECH_NS=mkpp_{mech}",
         f"-I{GEN}", f"-I{CSRC}", f"-I{INCLUDE}",
-        *(extra or []),
-        str(CSRC / "mkpp_capi.cu"), "-o", str(tmp),
     ]
+
+
+def _compile_unit(mech: str, unit: str, verbose: bool) -> Path:
+    obj = LIB / f"obj_{mech}" / unit.replace(".cu", ".o")
+    obj.parent.mkdir(parents=True, exist_ok=True)
+    tmp = obj.with_suffix(f".o.tmp{os.getpid()}")
+    cmd = [nvcc(), *_flags(mech, verbose), "-c", str(CSRC / unit), "-o", str(tmp)]
     proc = subprocess.run(cmd, capture_output=True, text=True)
     if proc.returncode != 0:
         tmp.unlink(missing_ok=True)
-        raise RuntimeError(f"nvcc failed for {mech}:\n{' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
+        raise RuntimeError(f"nvcc failed for {mech}/{unit}:\n{' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
     if verbose:
         sys.stderr.write(proc.stderr)
+    os.replace(tmp, obj)
+    return obj
+
+
+def _link(mech: str, objs: list[Path]) -> Path:
+    out = lib_path(mech)
+    tmp = out.with_suffix(f".so.tmp{os.getpid()}")
+    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *map(str, objs), "-o", str(tmp)]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        tmp.unlink(missing_ok=True)
+        raise RuntimeError(f"link failed for {mech}:\n{proc.stdout}\n{proc.stderr}")
     os.replace(tmp, out)
     return out
+
+
+def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    """Compile the units of one mechanism in parallel and link the library."""
+    LIB.mkdir(parents=True, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda u: _compile_unit(mech, u, verbose), UNITS))
+    return _link(mech, objs)
 
 
 def compile_probe() -> Path:

@@ -8,22 +8,13 @@
 // return codes.  mkpp_integrate stages the caller's host arrays to device
 // memory owned by the handle, runs the GPU solve on the handle's stream and
 // copies the concentrations back before returning.
-#include <cuda_runtime.h>
-
-#include <algorithm>
-#include <cmath>
-#include <cstdint>
-#include <cstdlib>
-#include <cstring>
 #include <cstdio>
 #include <mutex>
 #include <string>
 
-#include "../../include/mkpp.h"
-#include "solver.cuh"
-#include MKPP_MECH_HEADER
+#include "capi_common.cuh"
 
-using Mech = MKPP_MECH_NS::Mech;
+using namespace mkpp_tu;
 
 namespace {
 
@@ -87,10 +78,6 @@ int device_fail(mkpp_handle_s* h, cudaError_t err, const char* what) {
     if (e_ != cudaSuccess) return device_fail((h), e_, #call);  \
   } while (0)
 
-int launch_grid(size_t cells, int block) { return (int)std::max<size_t>(1, (cells + block - 1) / block); }
-
-using StoreInfo = mkpp::StoreFor<Mech>;
-constexpr size_t kQueueBytes = 256;
 
 // Launch configuration of the integrate kernels, process wide:
 //  register_variant  launch-bounds minimum of resident blocks (2: up to 255
@@ -147,15 +134,14 @@ const LaunchConfig& launch_config() {
     cudaDeviceGetAttribute(&cfg.sms, cudaDevAttrMultiProcessorCount, dev);
     cfg.sms = std::max(1, cfg.sms);
     cfg.minb = t.register_variant;
-    int per_sm = cfg.minb == 4 ? resident_blocks<4>() : resident_blocks<2>();
+    int per_sm = cfg.minb == 4 ? resident_blocks4() : resident_blocks<2>();
     if (t.blocks_per_sm > 0) per_sm = std::min(per_sm, t.blocks_per_sm);
     cfg.grid = cfg.sms * per_sm;
     // Cooperative kernel: as many warps per block as fit in 200 KB of shared memory.
     const size_t per_warp = (size_t)Mech::COOP_SLOTS * sizeof(double);
     cfg.coop_warps = (int)std::max<size_t>(1, std::min<size_t>(4, (200u * 1024u) / per_warp));
     cfg.coop_smem = per_warp * cfg.coop_warps;
-    cudaFuncSetAttribute(mkpp::integrate_coop_kernel<Mech>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)cfg.coop_smem);
+    set_coop_smem(cfg.coop_smem);
   }
   return cfg;
 }
@@ -200,103 +186,25 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
     a.defer_after = tuning().defer_after;
     a.defer = a.defer_after > 0 ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
     if (!a.defer) a.defer_after = 0;
-    if (cfg.minb == 4)
-      mkpp::integrate_persistent_kernel<Mech, 4><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
-    else
+    if (cfg.minb == 4) {
+      if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+    } else {
       mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+    }
     if (a.defer_after > 0) {
-      mkpp::integrate_coop_kernel<Mech><<<cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream>>>(a);
+      if (launch_coop(a, cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream) != MKPP_SUCCESS) {
+        return MKPP_ERROR_DEVICE;
+      }
     }
   } else {
     // The plain form runs with the same grid and the 255-register variant.
     a.defer = nullptr;
     a.defer_after = 0;
-    mkpp::integrate_plain_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+    if (launch_plain(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
   }
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
 
-mkpp::LaunchArgs make_args(size_t cells, double* conc, const double* ktab, int steps, double dt, double seed,
-                           int max_attempts, int* status, int* accepted, int* rejected) {
-  mkpp::LaunchArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.ncells = (int)cells;
-  a.steps = steps;
-  a.dt = dt;
-  a.seed = seed;
-  a.max_attempts = max_attempts;
-  a.conc = conc;
-  a.ktab = ktab;
-  a.status = status;
-  a.n_accept = accepted;
-  a.n_reject = rejected;
-  return a;
-}
-
-// ---------------------------------------------------------------------------
-// Tendency and dense-Jacobian evaluation (compute_rates / compute_jacobian,
-// src/mkpp/templates/kernel_functions/compute_{rates,jacobian}.j2).
-// ---------------------------------------------------------------------------
-// State accessor over a cell's row of the (species x cells) array.
-struct CellState {
-  const double* conc;
-  size_t c, n;
-  __device__ __forceinline__ double operator()(int i) const { return conc[c + n * Mech::var_phys(i)]; }
-};
-
-__global__ void __launch_bounds__(128, 1) eval_rates_kernel(size_t n, const double* conc, const double* ktab,
-                                                         double* out) {
-  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const mkpp::KTable k{ktab + c, n};
-  for (int s = 0; s < Mech::NS; ++s) out[c + n * s] = 0.0;
-  Mech::fun(CellState{conc, c, n}, k, [&](int i, double v) { out[c + n * Mech::var_phys(i)] = v; });
-}
-
-// Writes W slots straight into the dense (cells x N x N) LayoutLeft output.
-struct DenseSlots {
-  double* out;
-  size_t c, n;
-  __device__ __forceinline__ double& operator[](int s) const {
-    return out[c + n * ((size_t)Mech::lu_prow(s) + (size_t)Mech::NS * Mech::lu_pcol(s))];
-  }
-};
-
-__global__ void __launch_bounds__(128, 1) eval_jacobian_kernel(size_t n, const double* conc, const double* ktab,
-                                                            double* out) {
-  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const mkpp::KTable k{ktab + c, n};
-  const size_t NS = Mech::NS;
-  for (size_t e = 0; e < NS * NS; ++e) out[c + n * e] = 0.0;
-  DenseSlots S{out, c, n};
-  // W with inv_g_dt = 0 is -J on the W slots; flip the sign afterwards.
-  Mech::jac_w(CellState{conc, c, n}, k, 0.0, S);
-  Mech::for_each_w_slot([&](int slot, int, int) { S[slot] = -S[slot]; });
-}
-
-__global__ void __launch_bounds__(128, 1) mkpp_fixed_columns_kernel(size_t n, const double* conc, const double* temp,
-                                                                 const double* rho, const double* rh,
-                                                                 const double* clw, const double* param,
-                                                                 double* out) {
-  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const CellState y{conc, c, n};
-  const double T = (Mech::RUNTIME_ENV && temp) ? temp[c] : Mech::ENV_T;
-  const double RHO = (Mech::RUNTIME_ENV && rho) ? rho[c] : Mech::ENV_RHO;
-  const double RH = rh ? rh[c] : 0.5;
-  const double CLW = clw ? clw[c] : 0.0;
-  const mkpp::CellRow fix{conc + c, n};
-  const size_t NS = Mech::NS;
-  auto put = [&](int row, int col, double v) { out[c + n * (row + NS * col)] = v; };
-  if (param) {
-    const mkpp::CellRow P{param + c, n};
-    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
-  } else {
-    const mkpp::ZeroRow P;
-    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Allocation-free integrate (mkpp_gpu_integrate_noalloc).
@@ -356,9 +264,7 @@ int mkpp_gpu_integrate_noalloc(size_t num_cells, double* conc, const double* kta
   mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
   a.k_step_stride = k_step_stride;
   const int grid = (int)((num_cells + mkpp::kBlock - 1) / mkpp::kBlock);
-  mkpp::integrate_plain_kernel<Mech, 2><<<grid, mkpp::kBlock, 0, (cudaStream_t)stream>>>(
-      a, StoreInfo::kTile ? scratch : nullptr);
-  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+  return launch_plain(a, StoreInfo::kTile ? scratch : nullptr, grid, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -612,8 +518,8 @@ int mkpp_evaluate_rates(mkpp_handle_t handle, double* rates_out) {
   if (rc != MKPP_SUCCESS) return rc;
   rc = stage_inputs(h);
   if (rc != MKPP_SUCCESS) return rc;
-  eval_rates_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(n, h->dev.conc, h->dev.ktab, h->dev.out);
-  MKPP_CUDA(h, cudaGetLastError());
+  if (launch_eval_rates(n, h->dev.conc, h->dev.ktab, h->dev.out, h->stream) != MKPP_SUCCESS)
+    return device_fail(h, cudaGetLastError(), "eval_rates_kernel launch");
   MKPP_CUDA(h, cudaMemcpyAsync(rates_out, h->dev.out, bytes, cudaMemcpyDeviceToHost, h->stream));
   MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
   return MKPP_SUCCESS;
@@ -638,14 +544,13 @@ int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out) {
   if (rc != MKPP_SUCCESS) return rc;
   rc = stage_inputs(h);
   if (rc != MKPP_SUCCESS) return rc;
-  eval_jacobian_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(n, h->dev.conc, h->dev.ktab, h->dev.out);
-  MKPP_CUDA(h, cudaGetLastError());
-  if (Mech::NFIX > 0) {
-    mkpp_fixed_columns_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(
-        n, h->dev.conc, h->dev.temp, h->dev.rho, h->rh ? h->dev.rh : nullptr, h->clw ? h->dev.clw : nullptr,
-        h->param ? h->dev.param : nullptr, h->dev.out);
-    MKPP_CUDA(h, cudaGetLastError());
-  }
+  if (launch_eval_jacobian(n, h->dev.conc, h->dev.ktab, h->dev.out, h->stream) != MKPP_SUCCESS)
+    return device_fail(h, cudaGetLastError(), "eval_jacobian_kernel launch");
+  if (Mech::NFIX > 0 &&
+      launch_fixed_columns(n, h->dev.conc, h->dev.temp, h->dev.rho, h->rh ? h->dev.rh : nullptr,
+                           h->clw ? h->dev.clw : nullptr, h->param ? h->dev.param : nullptr, h->dev.out,
+                           h->stream) != MKPP_SUCCESS)
+    return device_fail(h, cudaGetLastError(), "fixed_columns_kernel launch");
   MKPP_CUDA(h, cudaMemcpyAsync(jac_out, h->dev.out, bytes, cudaMemcpyDeviceToHost, h->stream));
   MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
   return MKPP_SUCCESS;
@@ -772,23 +677,6 @@ int mkpp_gpu_integrate_logged(size_t num_cells, double* conc, const double* ktab
   a.log_n = log_n;
   a.log_cap = log_cap;
   return launch_integrate(a, 0, workspace, (cudaStream_t)stream);
-}
-
-int mkpp_gpu_evaluate_rates(size_t num_cells, const double* conc, const double* ktab, double* rates_out,
-                            void* stream) {
-  if (!conc || !ktab || !rates_out) return MKPP_ERROR_NULL_POINTER;
-  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
-  eval_rates_kernel<<<launch_grid(num_cells, 128), 128, 0, (cudaStream_t)stream>>>(num_cells, conc, ktab, rates_out);
-  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
-}
-
-int mkpp_gpu_evaluate_jacobian(size_t num_cells, const double* conc, const double* ktab, double* jac_out,
-                               void* stream) {
-  if (!conc || !ktab || !jac_out) return MKPP_ERROR_NULL_POINTER;
-  if (num_cells == 0) return MKPP_ERROR_INVALID_ARGUMENT;
-  eval_jacobian_kernel<<<launch_grid(num_cells, 128), 128, 0, (cudaStream_t)stream>>>(num_cells, conc, ktab,
-                                                                                      jac_out);
-  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
 
 }  // extern "C"

@@ -1,0 +1,20 @@
+// The warp-cooperative integrate of parked cells for one mechanism library,
+// in its own translation unit so it compiles in parallel with the other
+// kernels.
+#include "capi_common.cuh"
+
+namespace mkpp_tu {
+
+int set_coop_smem(size_t bytes) {
+  return cudaFuncSetAttribute(mkpp::integrate_coop_kernel<Mech>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes) == cudaSuccess
+             ? MKPP_SUCCESS
+             : MKPP_ERROR_DEVICE;
+}
+
+int launch_coop(const mkpp::LaunchArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
+  mkpp::integrate_coop_kernel<Mech><<<grid, threads, smem, stream>>>(a);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+}  // namespace mkpp_tu

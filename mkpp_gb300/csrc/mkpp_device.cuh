@@ -21,6 +21,7 @@ enum CellStatus : int {
   CELL_ERR_NON_FINITE_STATE = 2,
   CELL_ERR_CONVERGENCE_FAILURE = 3,
   CELL_ERR_NUMERICAL_FAILURE = 4,
+  CELL_ERR_CHECKPOINT_OVERFLOW = 5,   // more accepted steps than checkpoint slots
 };
 
 // Read-only strided view of one cell's row in a LayoutLeft (cells x n) array:

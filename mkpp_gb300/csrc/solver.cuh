@@ -472,4 +472,145 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
   }
 }
 
+// ---------------------------------------------------------------------------
+// Differentiation: forward with checkpoints at accepted steps, the discrete
+// adjoint sweep over them, and a replay of a frozen step sequence.
+// Checkpoint layout (cell index innermost): the state before accepted step s
+// at y[(s * NV + i) * ncells + c], its step size at h[s * ncells + c], the
+// number of accepted steps at n[c].
+// ---------------------------------------------------------------------------
+struct CheckpointArgs {
+  int cap;            // accepted steps a cell may record
+  double* y;
+  double* h;
+  int* n;
+};
+
+template <int N>
+struct StoreN {
+  static constexpr bool kTile = N > kRegisterSlots;
+  using type = typename std::conditional<kTile, TileStore, RegStore<(kTile ? 1 : N)>>::type;
+  static constexpr size_t block_bytes = kTile ? (size_t)N * kBlock * sizeof(double) : 0;
+  __device__ __forceinline__ static type make(double* scratch) {
+    type s{};
+    if constexpr (kTile) s.p = scratch + (size_t)blockIdx.x * N * kBlock + threadIdx.x;
+    return s;
+  }
+};
+
+// One integrate() call per cell (plain form) that records (y_n, h) at every
+// accepted step.  Same arithmetic as integrate_plain_kernel.
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 2) integrate_checkpoint_kernel(LaunchArgs a, CheckpointArgs ck,
+                                                                         double* scratch) {
+  using SN = StoreN<Mech::NSLOTS>;
+  typename SN::type S = SN::make(scratch);
+  const size_t n = (size_t)a.ncells;
+  const size_t T = (size_t)gridDim.x * kBlock;
+  for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
+    if (a.status && a.status[c] != CELL_SUCCESS) continue;
+    load_state<Mech>(a.conc, c, n, S);
+    load_rates<Mech>(a, c, 0, S);
+    auto k = [&](int r) { return S[Mech::KT + r]; };
+    Controller ctl;
+    ctl.start(a.dt, a.seed);
+    int nacc = 0, nrej = 0, cnt = 0;
+    bool capped = false, zero_pivot = false, overflow = false;
+    while (ctl.running()) {
+      if (ctl.attempts >= a.max_attempts) {
+        capped = true;
+        break;
+      }
+      const double h = ctl.next_h();
+      int st = 0;
+      const double err = Mech::attempt(S, k, h, st);
+      zero_pivot |= st != 0;
+      if (ctl.update<Mech>(err)) {
+        if (cnt >= ck.cap) {
+          overflow = true;
+          break;
+        }
+#pragma unroll 4
+        for (int i = 0; i < Mech::NV; ++i) ck.y[((size_t)cnt * Mech::NV + i) * n + c] = S[Mech::Y + i];
+        ck.h[(size_t)cnt * n + c] = h;
+        ++cnt;
+        apply_increment<Mech>(S);
+        ++nacc;
+      } else {
+        ++nrej;
+      }
+    }
+    store_state<Mech>(a.conc, c, n, S);
+    ck.n[c] = cnt;
+    const int status = overflow ? CELL_ERR_CHECKPOINT_OVERFLOW : final_status<Mech>(S, capped, zero_pivot);
+    if (a.status) a.status[c] = status;
+    if (a.n_accept) a.n_accept[c] = nacc;
+    if (a.n_reject) a.n_reject[c] = nrej;
+  }
+}
+
+// Applies the recorded accepted steps (frozen step sequence) to conc.
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 2) integrate_replay_kernel(LaunchArgs a, CheckpointArgs ck,
+                                                                     double* scratch) {
+  using SN = StoreN<Mech::NSLOTS>;
+  typename SN::type S = SN::make(scratch);
+  const size_t n = (size_t)a.ncells;
+  const size_t T = (size_t)gridDim.x * kBlock;
+  for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
+    load_state<Mech>(a.conc, c, n, S);
+    load_rates<Mech>(a, c, 0, S);
+    auto k = [&](int r) { return S[Mech::KT + r]; };
+    const int cnt = ck.n[c];
+    for (int s = 0; s < cnt; ++s) {
+      int st = 0;
+      (void)Mech::attempt(S, k, ck.h[(size_t)s * n + c], st);
+      apply_increment<Mech>(S);
+    }
+    store_state<Mech>(a.conc, c, n, S);
+  }
+}
+
+struct AdjointArgs {
+  int ncells;
+  const double* ktab;      // [NR][ncells]
+  const double* lam;       // [NS][ncells]  dL/dy at the end of the call
+  double* grad_conc;       // [NS][ncells]  dL/dy at the start (fixed species 0)
+  double* grad_k;          // [NR][ncells]  dL/dk
+};
+
+// Reverse sweep: for each accepted step, last to first, recompute the step
+// from its checkpoint with attempt() (bit-identical to the forward) and apply
+// Mech::adjoint_step.
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 2) adjoint_kernel(AdjointArgs a, CheckpointArgs ck, double* scratch) {
+  using SN = StoreN<Mech::NSLOTS_ADJ>;
+  typename SN::type S = SN::make(scratch);
+  const size_t n = (size_t)a.ncells;
+  const size_t T = (size_t)gridDim.x * kBlock;
+  for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
+#pragma unroll 4
+    for (int r = 0; r < Mech::NR; ++r) {
+      S[Mech::KT + r] = __ldg(a.ktab + (size_t)r * n + c);
+      S[Mech::KB + r] = 0.0;
+    }
+#pragma unroll 4
+    for (int i = 0; i < Mech::NV; ++i) S[Mech::LAM + i] = a.lam[c + n * Mech::var_phys(i)];
+    auto k = [&](int r) { return S[Mech::KT + r]; };
+    for (int s = ck.n[c] - 1; s >= 0; --s) {
+#pragma unroll 4
+      for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] = ck.y[((size_t)s * Mech::NV + i) * n + c];
+      const double h = ck.h[(size_t)s * n + c];
+      int st = 0;
+      (void)Mech::attempt(S, k, h, st);
+      Mech::adjoint_step(S, k, h);
+    }
+    for (int i = 0; i < Mech::NS; ++i) a.grad_conc[c + n * i] = 0.0;
+#pragma unroll 4
+    for (int i = 0; i < Mech::NV; ++i) a.grad_conc[c + n * Mech::var_phys(i)] = S[Mech::LAM + i];
+#pragma unroll 4
+    for (int r = 0; r < Mech::NR; ++r) a.grad_k[c + n * r] = S[Mech::KB + r];
+  }
+}
+
 }  // namespace mkpp

@@ -97,6 +97,9 @@ def _sum_expr(init: str | None, terms: list[tuple[float, str]]) -> str:
 
 
 ILP_GROUP = 8
+# Slot count above which the solver keeps a cell's working set in the global
+# tile rather than registers (kRegisterSlots in csrc/solver.cuh).
+REGISTER_SLOTS = 96
 
 
 def _interleave(c, plan, ops, operands, scale):
@@ -475,6 +478,207 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("  }")
 
 
+def _monomial_terms(reactants, v2l):
+    """Exponents {logical species: power} of a reaction's variable monomial."""
+    m = {}
+    for s_, pw in reactants:
+        m[v2l[s_]] = m.get(v2l[s_], 0) + pw
+    return m
+
+
+def _mono_expr(expo, yname):
+    """C expression of prod y^e (factors repeated), '1.0' if empty."""
+    fac = []
+    for j in sorted(expo):
+        fac += [f"{yname}{j}"] * expo[j]
+    return " * ".join(fac) if fac else "1.0"
+
+
+def _dmono(expo, j):
+    """(coefficient, exponents) of d/dy_j of prod y^e, or None."""
+    if expo.get(j, 0) == 0:
+        return None
+    e = dict(expo)
+    c = e[j]
+    e[j] -= 1
+    if e[j] == 0:
+        del e[j]
+    return float(c), e
+
+
+def _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots):
+    """Discrete adjoint of one accepted step (reverse of ``attempt``).
+
+    Given lambda = dL/dy_{n+1} in S[LAM..] and the stage values of the step
+    recomputed by ``attempt`` (LU of W, K_i, y_n), overwrite S[LAM..] with
+    dL/dy_n and add dL/dk to S[KB..].  W = I/(gamma h) - J(y_n, k) and
+    f = sum_r net_r k_r m_r(y) (mass action), so every derivative is a sum
+    over reactions: (df/dk)^T Fbar, J^T Fbar, and the W terms
+    u^T dJ v = sum_r k_r (net_r.u) (H_r v . dy + grad m_r . v dk_r/k_r).
+    """
+    v2l = plan.phys_to_var
+    LAM = nslots
+    KBAR = LAM + nv
+    FBAR = KBAR + stages * nv
+    KB = FBAR + nv
+    nadj = KB + nr
+    c("")
+    c("  // ---- discrete adjoint of one accepted step ----")
+    c(f"  static constexpr int LAM = {LAM};      // dL/dy")
+    c(f"  static constexpr int KBAR = {KBAR};    // stage adjoints, NSTAGE x NV")
+    c(f"  static constexpr int FBAR = {FBAR};    // adjoint of the pending stage tendency")
+    c(f"  static constexpr int KB = {KB};        // dL/dk accumulated")
+    c(f"  static constexpr int NSLOTS_ADJ = {nadj};")
+    # With the adjoint state in the global tile (more slots than the register
+    # store holds), the two largest adjoint-only helpers are compiled once as
+    # out-of-line functions instead of once per stage: this bounds the size
+    # of the adjoint kernel's body, which sets its compile time.  Register
+    # stores stay inlined, since a call would move them to local memory.
+    adj_inline = "__noinline__" if nadj > REGISTER_SLOTS else "__forceinline__"
+    # transposed solve: W^T x = b  with W = LU: U^T z = b (forward), L^T x = z (backward)
+    ucol = [[] for _ in range(nv)]   # U(k, i), k < i
+    lcol = [[] for _ in range(nv)]   # L(k, i), k > i
+    for (r_, cc), sl in plan.lu_index.items():
+        if r_ < cc:
+            ucol[cc].append((r_, sl))
+        elif r_ > cc:
+            lcol[cc].append((r_, sl))
+    c("  // Solve W^T x = b in place on [base, base + NV) with the stored LU of W.")
+    c("  template <class SA>")
+    c(f"  __device__ {adj_inline} static void solve_t(SA& S, const int base) {{")
+    for i in range(nv):
+        expr = f"S[base + {i}]"
+        for k_, sl in sorted(ucol[i]):
+            expr = f"fma(-S[{sl}], z{k_}, {expr})"
+        c(f"    const double z{i} = ({expr}) * S[{plan.diag[i]}];")
+    for i in range(nv - 1, -1, -1):
+        expr = f"z{i}"
+        for k_, sl in sorted(lcol[i]):
+            expr = f"fma(-S[{sl}], x{k_}, {expr})"
+        c(f"    const double x{i} = {expr};")
+        c(f"    S[base + {i}] = x{i};")
+    c("  }")
+    c("")
+    # per-reaction helpers
+    rx = []
+    for r in plan.reactions:
+        expo = _monomial_terms(r.reactants, v2l)
+        net = [(v2l[s_], co) for s_, co in r.net]
+        rx.append((r.index, expo, net))
+
+    def dot_net(net, uname):
+        terms = [(co, f"{uname}({i})") for i, co in net]
+        return _sum_expr(None, terms)
+
+    # W term: u^T dJ(y) v  -> dy and dk contributions
+    c("  // u^T J(y) v terms of stage i: y in S[Y..], u in S[ub..], v = K_i in S[vb..].")
+    c("  template <class SA, class KA>")
+    c(f"  __device__ {adj_inline} static void adj_wterm(SA& S, const KA& k, const int ub, const int vb) {{")
+    c("    auto u = [&](int i) { return S[ub + i]; };")
+    used = sorted({j for _, e, _ in rx for j in e})
+    for j in used:
+        c(f"    const double y{j} = S[Y + {j}];")
+        c(f"    const double v{j} = S[vb + {j}];")
+    acc_y = {}
+    for ri, expo, net in rx:
+        if not net or not expo:
+            continue
+        c(f"    {{ const double s = {dot_net(net, 'u')};")
+        # grad m . v
+        gterms = []
+        for j in sorted(expo):
+            d = _dmono(expo, j)
+            coef, e2 = d
+            gterms.append((coef, f"({_mono_expr(e2, 'y')}) * v{j}" if e2 else f"v{j}"))
+        c(f"      S[KB + {ri}] = fma(s, {_sum_expr(None, gterms)}, S[KB + {ri}]);")
+        c(f"      const double ks = k({ri}) * s;")
+        # H v: for each p: sum_q d2m/dy_p dy_q v_q
+        for p_ in sorted(expo):
+            d1 = _dmono(expo, p_)
+            hterms = []
+            for q in sorted(d1[1]):
+                d2 = _dmono(d1[1], q)
+                coef = d1[0] * d2[0]
+                hterms.append((coef, f"({_mono_expr(d2[1], 'y')}) * v{q}" if d2[1] else f"v{q}"))
+            if hterms:
+                c(f"      S[LAM + {p_}] = fma(ks, {_sum_expr(None, hterms)}, S[LAM + {p_}]);")
+        c("    }")
+    c("  }")
+    c("")
+    # F term at a stage state Y_i given Fbar: J(Y)^T Fbar into LAM and (df/dk)^T Fbar into KB,
+    # and the Y-adjoint returned through out(j, value) for the K_j contributions.
+    c("  // Adjoint of F_i = f(Y_i): Ybar = J(Y_i)^T Fbar, kbar += m_r(Y_i) (net_r.Fbar).")
+    c("  // yv(i) supplies Y_i, ybar(j, x) receives Ybar_j.")
+    c("  template <class SA, class KA, class YA, class OUT>")
+    c("  __device__ __forceinline__ static void adj_fterm(SA& S, const KA& k, const YA& yv, OUT&& ybar) {")
+    c("    auto fb = [&](int i) { return S[FBAR + i]; };")
+    for j in used:
+        c(f"    const double y{j} = yv({j});")
+    yb_terms = {j: [] for j in range(nv)}
+    for ri, expo, net in rx:
+        if not net:
+            continue
+        c(f"    const double s{ri} = {dot_net(net, 'fb')};")
+        c(f"    S[KB + {ri}] = fma(s{ri}, {_mono_expr(expo, 'y')}, S[KB + {ri}]);")
+        for j in sorted(expo):
+            coef, e2 = _dmono(expo, j)
+            mono = _mono_expr(e2, 'y')
+            t = f"k({ri}) * s{ri}" + ("" if mono == "1.0" else f" * {mono}")
+            yb_terms[j].append((coef, t))
+    for j in range(nv):
+        if yb_terms[j]:
+            c(f"    ybar({j}, {_sum_expr(None, yb_terms[j])});")
+    c("  }")
+    c("")
+    # adjoint step
+    c("  // Reverse of one accepted step of size h.  Requires the values attempt()")
+    c("  // left in S for this step (LU, K_i) and y_n in S[Y..].")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static void adjoint_step(SA& S, const KA& k, double h) {")
+    for i in range(stages):
+        mi = M[i]
+        c("    #pragma unroll")
+        c("    for (int j = 0; j < NV; ++j) S[KBAR + " + str(i * nv) + " + j] = "
+          + (f"{_lit(mi)} * S[LAM + j];" if mi != 0.0 else "0.0;"))
+    c("    #pragma unroll")
+    c("    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;")
+    # src stage for each stage's F
+    src = []
+    last = 0
+    for i in range(stages):
+        if NewF[i]:
+            last = i
+        src.append(last)
+    for i in range(stages - 1, -1, -1):
+        kb_i = f"KBAR + {i * nv}"
+        c(f"    // stage {i + 1}")
+        c(f"    solve_t(S, {kb_i});                       // u_i = W^-T Kbar_i")
+        c(f"    adj_wterm(S, k, {kb_i}, {K0 + i * nv});       // J(y_n) in W")
+        c("    #pragma unroll")
+        c(f"    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[{kb_i} + j];")
+        for j in range(i):
+            cv = C[i * (i - 1) // 2 + j]
+            if cv != 0.0:
+                c(f"    {{ const double cc = {_lit(cv)} / h;")
+                c("      #pragma unroll")
+                c(f"      for (int q = 0; q < NV; ++q) S[KBAR + {j * nv} + q] = fma(cc, S[{kb_i} + q], S[KBAR + {j * nv} + q]); }}")
+        if NewF[i]:
+            # Y_i = y_n + sum_j a_ij K_j
+            aterms = [(A[i * (i - 1) // 2 + j], j) for j in range(i) if i > 0 and A[i * (i - 1) // 2 + j] != 0.0]
+            yexpr = "S[Y + q]"
+            for a, j in aterms:
+                kk = f"S[{K0 + j * nv} + q]"
+                yexpr = f"{yexpr} + {kk}" if a == 1.0 else f"{yexpr} + {_lit(a)} * {kk}"
+            acc_lines = ["S[LAM + j] += x;"]
+            for a, j in aterms:
+                acc_lines.append(f"S[KBAR + {j * nv} + j] = fma({_lit(a)}, x, S[KBAR + {j * nv} + j]);")
+            c(f"    adj_fterm(S, k, [&](int q) {{ return {yexpr}; }},")
+            c(f"              [&](int j, double x) {{ {' '.join(acc_lines)} }});")
+            c("    #pragma unroll")
+            c("    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;")
+    c("  }")
+
+
 def emit_mechanism(plan: ReducedPlan) -> str:
     raw = plan.raw
     name = plan.name
@@ -824,6 +1028,7 @@ def emit_mechanism(plan: ReducedPlan) -> str:
     c("    return fmax(0.2, fmin(fac, 6.0));")
     c("  }")
     _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None)
+    _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots)
     c("};")
     c("")
     c(f"}}  // namespace mkpp_{name}")

@@ -413,6 +413,125 @@ struct Mech {
     }
     return __shfl_sync(0xffffffffu, err, 0);
   }
+
+  // ---- discrete adjoint of one accepted step ----
+  static constexpr int LAM = 31;      // dL/dy
+  static constexpr int KBAR = 34;    // stage adjoints, NSTAGE x NV
+  static constexpr int FBAR = 43;    // adjoint of the pending stage tendency
+  static constexpr int KB = 46;        // dL/dk accumulated
+  static constexpr int NSLOTS_ADJ = 50;
+  // Solve W^T x = b in place on [base, base + NV) with the stored LU of W.
+  template <class SA>
+  __device__ __forceinline__ static void solve_t(SA& S, const int base) {
+    const double z0 = (S[base + 0]) * S[0];
+    const double z1 = (fma(-S[1], z0, S[base + 1])) * S[4];
+    const double z2 = (fma(-S[5], z1, fma(-S[2], z0, S[base + 2]))) * S[8];
+    const double x2 = z2;
+    S[base + 2] = x2;
+    const double x1 = fma(-S[7], x2, z1);
+    S[base + 1] = x1;
+    const double x0 = fma(-S[6], x2, fma(-S[3], x1, z0));
+    S[base + 0] = x0;
+  }
+
+  // u^T J(y) v terms of stage i: y in S[Y..], u in S[ub..], v = K_i in S[vb..].
+  template <class SA, class KA>
+  __device__ __forceinline__ static void adj_wterm(SA& S, const KA& k, const int ub, const int vb) {
+    auto u = [&](int i) { return S[ub + i]; };
+    const double y0 = S[Y + 0];
+    const double v0 = S[vb + 0];
+    const double y1 = S[Y + 1];
+    const double v1 = S[vb + 1];
+    const double y2 = S[Y + 2];
+    const double v2 = S[vb + 2];
+    { const double s = fma(2.0, u(1), -u(2));
+      S[KB + 0] = fma(s, v2, S[KB + 0]);
+      const double ks = k(0) * s;
+    }
+    { const double s = -u(1) - u(2) + u(0);
+      S[KB + 1] = fma(s, (y2) * v1 + (y1) * v2, S[KB + 1]);
+      const double ks = k(1) * s;
+      S[LAM + 1] = fma(ks, v2, S[LAM + 1]);
+      S[LAM + 2] = fma(ks, v1, S[LAM + 2]);
+    }
+    { const double s = -u(0) + u(1) + u(2);
+      S[KB + 2] = fma(s, v0, S[KB + 2]);
+      const double ks = k(2) * s;
+    }
+    { const double s = fma(2.0, u(2), -u(1) - u(0));
+      S[KB + 3] = fma(s, (y1) * v0 + (y0) * v1, S[KB + 3]);
+      const double ks = k(3) * s;
+      S[LAM + 0] = fma(ks, v1, S[LAM + 0]);
+      S[LAM + 1] = fma(ks, v0, S[LAM + 1]);
+    }
+  }
+
+  // Adjoint of F_i = f(Y_i): Ybar = J(Y_i)^T Fbar, kbar += m_r(Y_i) (net_r.Fbar).
+  // yv(i) supplies Y_i, ybar(j, x) receives Ybar_j.
+  template <class SA, class KA, class YA, class OUT>
+  __device__ __forceinline__ static void adj_fterm(SA& S, const KA& k, const YA& yv, OUT&& ybar) {
+    auto fb = [&](int i) { return S[FBAR + i]; };
+    const double y0 = yv(0);
+    const double y1 = yv(1);
+    const double y2 = yv(2);
+    const double s0 = fma(2.0, fb(1), -fb(2));
+    S[KB + 0] = fma(s0, y2, S[KB + 0]);
+    const double s1 = -fb(1) - fb(2) + fb(0);
+    S[KB + 1] = fma(s1, y1 * y2, S[KB + 1]);
+    const double s2 = -fb(0) + fb(1) + fb(2);
+    S[KB + 2] = fma(s2, y0, S[KB + 2]);
+    const double s3 = fma(2.0, fb(2), -fb(1) - fb(0));
+    S[KB + 3] = fma(s3, y0 * y1, S[KB + 3]);
+    ybar(0, k(2) * s2 + k(3) * s3 * y1);
+    ybar(1, k(1) * s1 * y2 + k(3) * s3 * y0);
+    ybar(2, k(0) * s0 + k(1) * s1 * y1);
+  }
+
+  // Reverse of one accepted step of size h.  Requires the values attempt()
+  // left in S for this step (LU, K_i) and y_n in S[Y..].
+  template <class SA, class KA>
+  __device__ __forceinline__ static void adjoint_step(SA& S, const KA& k, double h) {
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 0 + j] = 1.0 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 3 + j] = 6.1697947043828245 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 6 + j] = -0.42772256543218573 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+    // stage 3
+    solve_t(S, KBAR + 6);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 6, 18);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 6 + j];
+    { const double cc = 4.0759956452537702 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 0 + q] = fma(cc, S[KBAR + 6 + q], S[KBAR + 0 + q]); }
+    { const double cc = 9.20767942983308 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 3 + q] = fma(cc, S[KBAR + 6 + q], S[KBAR + 3 + q]); }
+    // stage 2
+    solve_t(S, KBAR + 3);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 3, 15);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 3 + j];
+    { const double cc = -1.0156171083877703 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 0 + q] = fma(cc, S[KBAR + 3 + q], S[KBAR + 0 + q]); }
+    adj_fterm(S, k, [&](int q) { return S[Y + q] + S[12 + q]; },
+              [&](int j, double x) { S[LAM + j] += x; S[KBAR + 0 + j] = fma(1.0, x, S[KBAR + 0 + j]); });
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+    // stage 1
+    solve_t(S, KBAR + 0);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 0, 12);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 0 + j];
+    adj_fterm(S, k, [&](int q) { return S[Y + q]; },
+              [&](int j, double x) { S[LAM + j] += x; });
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+  }
 };
 
 }  // namespace mkpp_chapman

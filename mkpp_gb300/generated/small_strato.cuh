@@ -566,6 +566,188 @@ struct Mech {
     }
     return __shfl_sync(0xffffffffu, err, 0);
   }
+
+  // ---- discrete adjoint of one accepted step ----
+  static constexpr int LAM = 75;      // dL/dy
+  static constexpr int KBAR = 81;    // stage adjoints, NSTAGE x NV
+  static constexpr int FBAR = 99;    // adjoint of the pending stage tendency
+  static constexpr int KB = 105;        // dL/dk accumulated
+  static constexpr int NSLOTS_ADJ = 115;
+  // Solve W^T x = b in place on [base, base + NV) with the stored LU of W.
+  template <class SA>
+  __device__ __noinline__ static void solve_t(SA& S, const int base) {
+    const double z0 = (S[base + 0]) * S[0];
+    const double z1 = (S[base + 1]) * S[3];
+    const double z2 = (fma(-S[4], z1, S[base + 2])) * S[9];
+    const double z3 = (fma(-S[10], z2, fma(-S[5], z1, fma(-S[1], z0, S[base + 3])))) * S[16];
+    const double z4 = (fma(-S[17], z3, fma(-S[11], z2, S[base + 4]))) * S[22];
+    const double z5 = (fma(-S[23], z4, fma(-S[18], z3, fma(-S[12], z2, fma(-S[6], z1, S[base + 5]))))) * S[28];
+    const double x5 = z5;
+    S[base + 5] = x5;
+    const double x4 = fma(-S[27], x5, z4);
+    S[base + 4] = x4;
+    const double x3 = fma(-S[26], x5, fma(-S[21], x4, z3));
+    S[base + 3] = x3;
+    const double x2 = fma(-S[25], x5, fma(-S[20], x4, fma(-S[15], x3, z2)));
+    S[base + 2] = x2;
+    const double x1 = fma(-S[24], x5, fma(-S[19], x4, fma(-S[14], x3, fma(-S[8], x2, z1))));
+    S[base + 1] = x1;
+    const double x0 = fma(-S[13], x3, fma(-S[7], x2, fma(-S[2], x1, z0)));
+    S[base + 0] = x0;
+  }
+
+  // u^T J(y) v terms of stage i: y in S[Y..], u in S[ub..], v = K_i in S[vb..].
+  template <class SA, class KA>
+  __device__ __noinline__ static void adj_wterm(SA& S, const KA& k, const int ub, const int vb) {
+    auto u = [&](int i) { return S[ub + i]; };
+    const double y0 = S[Y + 0];
+    const double v0 = S[vb + 0];
+    const double y1 = S[Y + 1];
+    const double v1 = S[vb + 1];
+    const double y2 = S[Y + 2];
+    const double v2 = S[vb + 2];
+    const double y3 = S[Y + 3];
+    const double v3 = S[vb + 3];
+    const double y4 = S[Y + 4];
+    const double v4 = S[vb + 4];
+    const double y5 = S[Y + 5];
+    const double v5 = S[vb + 5];
+    { const double s = fma(2.0, u(1), -u(2));
+      S[KB + 0] = fma(s, v2, S[KB + 0]);
+      const double ks = k(0) * s;
+    }
+    { const double s = -u(1) - u(2) + u(3);
+      S[KB + 1] = fma(s, (y2) * v1 + (y1) * v2, S[KB + 1]);
+      const double ks = k(1) * s;
+      S[LAM + 1] = fma(ks, v2, S[LAM + 1]);
+      S[LAM + 2] = fma(ks, v1, S[LAM + 2]);
+    }
+    { const double s = -u(3) + u(1) + u(2);
+      S[KB + 2] = fma(s, v3, S[KB + 2]);
+      const double ks = k(2) * s;
+    }
+    { const double s = fma(2.0, u(2), -u(1) - u(3));
+      S[KB + 3] = fma(s, (y3) * v1 + (y1) * v3, S[KB + 3]);
+      const double ks = k(3) * s;
+      S[LAM + 1] = fma(ks, v3, S[LAM + 1]);
+      S[LAM + 3] = fma(ks, v1, S[LAM + 3]);
+    }
+    { const double s = -u(3) + u(0) + u(2);
+      S[KB + 4] = fma(s, v3, S[KB + 4]);
+      const double ks = k(4) * s;
+    }
+    { const double s = -u(0) + u(1);
+      S[KB + 5] = fma(s, v0, S[KB + 5]);
+      const double ks = k(5) * s;
+    }
+    { const double s = fma(2.0, u(2), -u(0) - u(3));
+      S[KB + 6] = fma(s, (y3) * v0 + (y0) * v3, S[KB + 6]);
+      const double ks = k(6) * s;
+      S[LAM + 0] = fma(ks, v3, S[LAM + 0]);
+      S[LAM + 3] = fma(ks, v0, S[LAM + 3]);
+    }
+    { const double s = -u(4) - u(3) + u(5) + u(2);
+      S[KB + 7] = fma(s, (y4) * v3 + (y3) * v4, S[KB + 7]);
+      const double ks = k(7) * s;
+      S[LAM + 3] = fma(ks, v4, S[LAM + 3]);
+      S[LAM + 4] = fma(ks, v3, S[LAM + 4]);
+    }
+    { const double s = -u(5) - u(1) + u(4) + u(2);
+      S[KB + 8] = fma(s, (y5) * v1 + (y1) * v5, S[KB + 8]);
+      const double ks = k(8) * s;
+      S[LAM + 1] = fma(ks, v5, S[LAM + 1]);
+      S[LAM + 5] = fma(ks, v1, S[LAM + 5]);
+    }
+    { const double s = -u(5) + u(4) + u(1);
+      S[KB + 9] = fma(s, v5, S[KB + 9]);
+      const double ks = k(9) * s;
+    }
+  }
+
+  // Adjoint of F_i = f(Y_i): Ybar = J(Y_i)^T Fbar, kbar += m_r(Y_i) (net_r.Fbar).
+  // yv(i) supplies Y_i, ybar(j, x) receives Ybar_j.
+  template <class SA, class KA, class YA, class OUT>
+  __device__ __forceinline__ static void adj_fterm(SA& S, const KA& k, const YA& yv, OUT&& ybar) {
+    auto fb = [&](int i) { return S[FBAR + i]; };
+    const double y0 = yv(0);
+    const double y1 = yv(1);
+    const double y2 = yv(2);
+    const double y3 = yv(3);
+    const double y4 = yv(4);
+    const double y5 = yv(5);
+    const double s0 = fma(2.0, fb(1), -fb(2));
+    S[KB + 0] = fma(s0, y2, S[KB + 0]);
+    const double s1 = -fb(1) - fb(2) + fb(3);
+    S[KB + 1] = fma(s1, y1 * y2, S[KB + 1]);
+    const double s2 = -fb(3) + fb(1) + fb(2);
+    S[KB + 2] = fma(s2, y3, S[KB + 2]);
+    const double s3 = fma(2.0, fb(2), -fb(1) - fb(3));
+    S[KB + 3] = fma(s3, y1 * y3, S[KB + 3]);
+    const double s4 = -fb(3) + fb(0) + fb(2);
+    S[KB + 4] = fma(s4, y3, S[KB + 4]);
+    const double s5 = -fb(0) + fb(1);
+    S[KB + 5] = fma(s5, y0, S[KB + 5]);
+    const double s6 = fma(2.0, fb(2), -fb(0) - fb(3));
+    S[KB + 6] = fma(s6, y0 * y3, S[KB + 6]);
+    const double s7 = -fb(4) - fb(3) + fb(5) + fb(2);
+    S[KB + 7] = fma(s7, y3 * y4, S[KB + 7]);
+    const double s8 = -fb(5) - fb(1) + fb(4) + fb(2);
+    S[KB + 8] = fma(s8, y1 * y5, S[KB + 8]);
+    const double s9 = -fb(5) + fb(4) + fb(1);
+    S[KB + 9] = fma(s9, y5, S[KB + 9]);
+    ybar(0, k(5) * s5 + k(6) * s6 * y3);
+    ybar(1, k(1) * s1 * y2 + k(3) * s3 * y3 + k(8) * s8 * y5);
+    ybar(2, k(0) * s0 + k(1) * s1 * y1);
+    ybar(3, k(2) * s2 + k(3) * s3 * y1 + k(4) * s4 + k(6) * s6 * y0 + k(7) * s7 * y4);
+    ybar(4, k(7) * s7 * y3);
+    ybar(5, k(8) * s8 * y1 + k(9) * s9);
+  }
+
+  // Reverse of one accepted step of size h.  Requires the values attempt()
+  // left in S for this step (LU, K_i) and y_n in S[Y..].
+  template <class SA, class KA>
+  __device__ __forceinline__ static void adjoint_step(SA& S, const KA& k, double h) {
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 0 + j] = 1.0 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 6 + j] = 6.1697947043828245 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[KBAR + 12 + j] = -0.42772256543218573 * S[LAM + j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+    // stage 3
+    solve_t(S, KBAR + 12);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 12, 47);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 12 + j];
+    { const double cc = 4.0759956452537702 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 0 + q] = fma(cc, S[KBAR + 12 + q], S[KBAR + 0 + q]); }
+    { const double cc = 9.20767942983308 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 6 + q] = fma(cc, S[KBAR + 12 + q], S[KBAR + 6 + q]); }
+    // stage 2
+    solve_t(S, KBAR + 6);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 6, 41);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 6 + j];
+    { const double cc = -1.0156171083877703 / h;
+      #pragma unroll
+      for (int q = 0; q < NV; ++q) S[KBAR + 0 + q] = fma(cc, S[KBAR + 6 + q], S[KBAR + 0 + q]); }
+    adj_fterm(S, k, [&](int q) { return S[Y + q] + S[35 + q]; },
+              [&](int j, double x) { S[LAM + j] += x; S[KBAR + 0 + j] = fma(1.0, x, S[KBAR + 0 + j]); });
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+    // stage 1
+    solve_t(S, KBAR + 0);                       // u_i = W^-T Kbar_i
+    adj_wterm(S, k, KBAR + 0, 35);       // J(y_n) in W
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] += S[KBAR + 0 + j];
+    adj_fterm(S, k, [&](int q) { return S[Y + q]; },
+              [&](int j, double x) { S[LAM + j] += x; });
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) S[FBAR + j] = 0.0;
+  }
 };
 
 }  // namespace mkpp_small_strato
