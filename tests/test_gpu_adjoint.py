@@ -3,7 +3,10 @@
 Checks, with the accepted-step sequence of the checkpointed forward frozen:
 * against a dense FP64 CPU discrete adjoint (oracle/adjoint_ref.py) of the same
   steps: gradients w.r.t. the initial state and the rate constants agree to
-  1e-8 of the cell's largest |x * dL/dx| (scale-free sensitivities);
+  1e-8 of the cell's largest |x * dL/dx| (scale-free sensitivities), or to
+  8x the cell's round-off floor where that is larger.  The floor is how far
+  the dense adjoint itself moves when k and y0 are perturbed by one ulp: up
+  to 3e-8 on stiff SAPRC99 cells (seeded case), 1e-12 on others;
 * against central finite differences (h = 1e-6 relative) of the loss
   L = sum_c (O3_c(dt) - target_c)^2 through the GPU replay of the same steps;
 * the torch.autograd.Function returns those gradients and the same forward
@@ -42,6 +45,24 @@ def _case(mech, n):
     return w, s, conc0, conc, ktab, ck
 
 
+def _roundoff_floor(dm, y0, k, hs, lam, g0, gk0, trials=2):
+    """Largest relative change of the dense adjoint under one-ulp perturbations
+    of k and y0 (same step sequence): the agreement two correct FP64
+    implementations can be expected to reach on this cell."""
+    rng = np.random.default_rng(11)
+    sy = max(np.abs(g0 * y0).max(), 1e-300)
+    sk = max(np.abs(gk0 * k).max(), 1e-300)
+    fy = fk = 0.0
+    for _ in range(trials):
+        kp = k * (1.0 + rng.integers(-1, 2, size=k.size) * 2.0**-52)
+        yp = y0 * (1.0 + rng.integers(-1, 2, size=y0.size) * 2.0**-52)
+        _, tape = dm.forward(yp, kp, hs)
+        g1, gk1 = dm.adjoint(kp, tape, lam)
+        fy = max(fy, np.abs((g1 - g0) * y0).max() / sy)
+        fk = max(fk, np.abs((gk1 - gk0) * k).max() / sk)
+    return fy, fk
+
+
 @pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99"])
 def test_adjoint_matches_dense_cpu_adjoint(built_libs, mech):
     import torch
@@ -67,11 +88,11 @@ def test_adjoint_matches_dense_cpu_adjoint(built_libs, mech):
         yT_cpu, tape = dm.forward(y0, k[:, c], hs_all[: cnt[c], c])
         np.testing.assert_allclose(yT_cpu, yT[vp, c], rtol=1e-9, atol=1e-6)
         g0, gkc = dm.adjoint(k[:, c], tape, lam[vp, c])
-        sy = np.abs(g0 * y0)
-        scale = max(sy.max(), 1e-300)
-        assert np.max(np.abs((gc[vp, c] - g0) * y0)) <= 1e-8 * scale
-        sk = np.abs(gkc * k[:, c])
-        assert np.max(np.abs((gk[:, c] - gkc) * k[:, c])) <= 1e-8 * max(sk.max(), 1e-300)
+        scale = max(np.abs(g0 * y0).max(), 1e-300)
+        sk = max(np.abs(gkc * k[:, c]).max(), 1e-300)
+        floor_y, floor_k = _roundoff_floor(dm, y0, k[:, c], hs_all[: cnt[c], c], lam[vp, c], g0, gkc)
+        assert np.max(np.abs((gc[vp, c] - g0) * y0)) <= max(1e-8, 8 * floor_y) * scale
+        assert np.max(np.abs((gk[:, c] - gkc) * k[:, c])) <= max(1e-8, 8 * floor_k) * sk
 
 
 @pytest.mark.parametrize("mech", ["small_strato", "saprc99"])
@@ -81,7 +102,9 @@ def test_adjoint_matches_central_differences(built_libs, mech):
     n = 64
     w, s, conc0, conc, ktab, ck = _case(mech, n)
     ok = (ck.status == 0).cpu().numpy()
-    o3 = list(w.conc.shape and __import__("mkpp_gb300.emitter.plan", fromlist=["load_raw"]).load_raw(mech)["species"]).index("O3")
+    from mkpp_gb300.emitter.plan import load, load_raw
+
+    o3 = load_raw(mech)["species"].index("O3")
     target = (conc[o3] * 1.1).clone()
 
     def loss(cend):
@@ -91,8 +114,6 @@ def test_adjoint_matches_central_differences(built_libs, mech):
     lam[o3] = 2.0 * (conc[o3] - target)
     gc, gk = ck.adjoint(ktab, lam)
     torch.cuda.synchronize()
-    from mkpp_gb300.emitter.plan import load
-
     vp = load(mech).var_phys
     rng = np.random.default_rng(5)
     species = [o3] + list(rng.choice(vp, size=4, replace=False))
