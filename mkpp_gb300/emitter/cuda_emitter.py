@@ -29,6 +29,7 @@ from __future__ import annotations
 import re
 from pathlib import Path
 
+from . import warp_schedule
 from .plan import ReducedPlan, load
 
 GEN_DIR = Path(__file__).resolve().parent.parent / "generated"
@@ -142,6 +143,15 @@ def _c_array(c, ctype, name, values):
     c(f"static __device__ const {ctype} {name}[{len(vals)}] = {{{body}}};")
 
 
+def _c_u64_array(c, name, values):
+    vals = list(values) or [0]
+    rows = [", ".join(f"0x{v:x}ull" for v in vals[i:i + 8]) for i in range(0, len(vals), 8)]
+    c(f"static __device__ const unsigned long long {name}[{len(vals)}] = {{")
+    for r in rows:
+        c(f"    {r},")
+    c("};")
+
+
 def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None):
     """Warp-cooperative form of one attempt: the same arithmetic, element by
     element, as ``attempt`` (same operand order in every sum and product), with
@@ -202,64 +212,14 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
             w_p.append(pi)
             w_c.append(_lit(coef))
         w_off.append(len(w_p))
-    # --- LU ops by level; kind 0 = plain, 1 = pivot (store 1/u), 2 = L (times 1/U_jj)
-    diag_slots = set(plan.diag)
-    slot_level = {}
-    op_level = []
-    for out, w, b, e, dg in plan.ops:
-        deps = [slot_level[x] for q in range(b, e) for x in plan.products[q]]
-        if dg >= 0:
-            deps.append(slot_level[dg])
-        L = 1 + max(deps) if deps else 0
-        slot_level[out] = L
-        op_level.append(L)
-    nlev = max(op_level) + 1
-    order = sorted(range(len(plan.ops)), key=lambda i: (op_level[i], -(plan.ops[i][3] - plan.ops[i][2]), i))
-    lu_lev_off = [0] * (nlev + 1)
-    for i in order:
-        lu_lev_off[op_level[i] + 1] += 1
-    for l in range(nlev):
-        lu_lev_off[l + 1] += lu_lev_off[l]
-    op_out, op_w, op_b, op_e, op_kind, op_dg = [], [], [], [], [], []
-    for i in order:
-        out, w, b, e, dg = plan.ops[i]
-        op_out.append(out)
-        op_w.append(int(w >= 0))
-        op_b.append(b)
-        op_e.append(e)
-        op_kind.append(1 if out in diag_slots else (2 if dg >= 0 else 0))
-        op_dg.append(dg if dg >= 0 else 0)
-    prod_l = [a for a, _ in plan.products]
-    prod_r = [b for _, b in plan.products]
-    # --- solves by level
-    fl = _levels(lambda i: [cc for cc, _ in plan.lower[i]], nv)
-    nfl = max(fl) + 1
-    bl_rev = [0] * nv
-    for i in range(nv - 1, -1, -1):
-        bl_rev[i] = 1 + max((bl_rev[cc] for cc, _ in plan.upper[i]), default=-1)
-    nbl = max(bl_rev) + 1
-    def lev_rows(levs, nl):
-        rows = sorted(range(nv), key=lambda i: (levs[i], i))
-        off = [0] * (nl + 1)
-        for i in rows:
-            off[levs[i] + 1] += 1
-        for l in range(nl):
-            off[l + 1] += off[l]
-        return rows, off
-    f_rows, f_lev_off = lev_rows(fl, nfl)
-    b_rows, b_lev_off = lev_rows(bl_rev, nbl)
-    lo_off, lo_col, lo_slot, up_off, up_col, up_slot = [0], [], [], [0], [], []
-    for i in range(nv):
-        for cc, sl in plan.lower[i]:
-            lo_col.append(cc)
-            lo_slot.append(sl)
-        lo_off.append(len(lo_col))
-        for cc, sl in plan.upper[i]:
-            up_col.append(cc)
-            up_slot.append(sl)
-        up_off.append(len(up_col))
+    # --- LU and solves: static 32-lane schedules of single multiply-adds
+    lu_prog = warp_schedule.lu_program(plan)
+    lu_steps = warp_schedule.schedule(lu_prog)
+    sv_prog = warp_schedule.solve_program(plan)
+    sv_steps = warp_schedule.schedule(sv_prog, relative=True)
+    lu_zero = warp_schedule.lu_zero_slots(plan)
     c("")
-    c("  // ---- warp-cooperative attempt (tables + level schedules) ----")
+    c("  // ---- warp-cooperative attempt (tables + static warp schedules) ----")
     c(f"  static constexpr int NPART = {npart};")
     nq = max(nr, nv)
     c(f"  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm")
@@ -284,29 +244,13 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     _c_array(c, "int", "w_off", w_off)
     _c_array(c, "int", "w_p", w_p)
     _c_array(c, "double", "w_c", w_c)
-    c(f"constexpr int LU_LEVELS = {nlev};")
     c(f"constexpr int NW = {len(w_slot)};")
-    _c_array(c, "int", "lu_lev_off", lu_lev_off)
-    _c_array(c, "int", "op_out", op_out)
-    _c_array(c, "int", "op_w", op_w)
-    _c_array(c, "int", "op_b", op_b)
-    _c_array(c, "int", "op_e", op_e)
-    _c_array(c, "int", "op_kind", op_kind)
-    _c_array(c, "int", "op_dg", op_dg)
-    c(f"static __device__ const int2 prod[{max(1, len(prod_l))}] = {{"
-      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(prod_l, prod_r)) + "};")
-    c(f"constexpr int F_LEVELS = {nfl};")
-    c(f"constexpr int B_LEVELS = {nbl};")
-    _c_array(c, "int", "f_rows", f_rows)
-    _c_array(c, "int", "f_lev_off", f_lev_off)
-    _c_array(c, "int", "b_rows", b_rows)
-    _c_array(c, "int", "b_lev_off", b_lev_off)
-    _c_array(c, "int", "lo_off", lo_off)
-    c(f"static __device__ const int2 lo[{max(1, len(lo_col))}] = {{"
-      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(lo_slot, lo_col)) + "};")
-    _c_array(c, "int", "up_off", up_off)
-    c(f"static __device__ const int2 up[{max(1, len(up_col))}] = {{"
-      + ", ".join(f"{{{a}, {b}}}" for a, b in zip(up_slot, up_col)) + "};")
+    c(f"constexpr int N_LU_ZERO = {len(lu_zero)};")
+    _c_array(c, "int", "lu_zero", lu_zero)
+    c(f"constexpr int LU_STEPS = {len(lu_steps)};")
+    c(f"constexpr int SV_STEPS = {len(sv_steps)};")
+    _c_u64_array(c, "lu_fs", warp_schedule.encode(lu_prog, lu_steps))
+    _c_u64_array(c, "sv_fs", warp_schedule.encode(sv_prog, sv_steps))
     _c_array(c, "int", "diag", plan.diag)
     c("}  // namespace coop")
     c("")
@@ -336,31 +280,45 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("    __syncwarp();")
     c("  }")
     c("")
-    c("  // Solve (LU) x = b in place on S[base..] by dependency levels.")
+    c("  // Run a static warp schedule (emitter/warp_schedule.py) on S: one")
+    c("  // multiply-add, pivot multiply or reciprocal per lane and step, a warp")
+    c("  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by")
+    c("  // base.  The next two steps' words are in flight while one executes.")
+    c("  // Returns false if a reciprocal met a zero pivot.")
+    c("  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,")
+    c("                                                     int steps, int base, unsigned lane) {")
+    c("    bool ok = true;")
+    c("    unsigned long long cur = __ldg(T + lane);")
+    c("    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;")
+    c("    for (int s = 0; s < steps; ++s) {")
+    c("      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;")
+    c("      const int kind = (int)(cur >> 48) & 3;")
+    c("      if (kind != 0) {")
+    c("        const int out = (int)(cur & 0xffffu) + base;")
+    c("        const int ia = (int)((cur >> 16) & 0xffffu);")
+    c("        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);")
+    c("        const double vo = S[out];")
+    c("        if (kind == 3) {")
+    c("          ok = ok && (vo != 0.0);")
+    c("          S[out] = 1.0 / vo;")
+    c("        } else {")
+    c("          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.")
+    c("          const double vb = S[ib];")
+    c("          const double x = kind == 1 ? -S[ia] : vo;")
+    c("          const double z = kind == 1 ? vo : -0.0;")
+    c("          S[out] = fma(x, vb, z);")
+    c("        }")
+    c("      }")
+    c("      __syncwarp();")
+    c("      cur = nxt;")
+    c("      nxt = nn;")
+    c("    }")
+    c("    return ok;")
+    c("  }")
+    c("")
+    c("  // Solve (LU) x = b in place on S[base..].")
     c("  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {")
-    c("    namespace T = coop;")
-    c("    for (int l = 0; l < T::F_LEVELS; ++l) {")
-    c("      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {")
-    c("        const int i = T::f_rows[j];")
-    c("        double v = S[base + i];")
-    c("        const int e1 = T::lo_off[i + 1];")
-    c("        #pragma unroll 4")
-    c("        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }")
-    c("        S[base + i] = v;")
-    c("      }")
-    c("      __syncwarp();")
-    c("    }")
-    c("    for (int l = 0; l < T::B_LEVELS; ++l) {")
-    c("      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {")
-    c("        const int i = T::b_rows[j];")
-    c("        double v = S[base + i];")
-    c("        const int e1 = T::up_off[i + 1];")
-    c("        #pragma unroll 4")
-    c("        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }")
-    c("        S[base + i] = v * S[T::diag[i]];")
-    c("      }")
-    c("      __syncwarp();")
-    c("    }")
+    c("    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);")
     c("  }")
     c("")
     c("  // One attempt by a whole warp on the cell held in shared memory S")
@@ -381,6 +339,7 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("      S[D + p] = d;")
     c("    }")
     c("    __syncwarp();")
+    c("    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;")
     c("    for (int w = lane; w < T::NW; w += 32) {")
     c("      bool first = !T::w_diag[w];")
     c("      double v = T::w_diag[w] ? inv_g_dt : 0.0;")
@@ -391,22 +350,8 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots,
     c("      S[T::w_slot[w]] = v;")
     c("    }")
     c("    __syncwarp();")
-    c("    // LU by dependency levels.")
-    c("    bool ok = true;")
-    c("    for (int l = 0; l < T::LU_LEVELS; ++l) {")
-    c("      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {")
-    c("        const int out = T::op_out[j];")
-    c("        double v = T::op_w[j] ? S[out] : 0.0;")
-    c("        const int q1 = T::op_e[j];")
-    c("        #pragma unroll 4")
-    c("        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }")
-    c("        const int kind = T::op_kind[j];")
-    c("        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }")
-    c("        else if (kind == 2) S[out] = v * S[T::op_dg[j]];")
-    c("        else S[out] = v;")
-    c("      }")
-    c("      __syncwarp();")
-    c("    }")
+    c("    // LU by the static warp schedule (fill-in slots were zeroed with W).")
+    c("    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);")
     c("    if (__any_sync(0xffffffffu, !ok)) status |= 1;")
     cur_f = None
     for st in range(1, stages + 1):

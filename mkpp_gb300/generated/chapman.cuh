@@ -21,26 +21,75 @@ static __device__ const int w_diag[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
 static __device__ const int w_off[10] = {0, 2, 4, 5, 7, 9, 11, 13, 15, 17};
 static __device__ const int w_p[17] = {3, 5, 1, 4, 2, 3, 5, 1, 4, 0, 2, 3, 5, 1, 4, 0, 2};
 static __device__ const double w_c[17] = {1.0, 1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 1.0, 1.0, -2.0, 1.0, -1.0, -2.0, 1.0, -2.0, 1.0, 1.0};
-constexpr int LU_LEVELS = 5;
 constexpr int NW = 9;
-static __device__ const int lu_lev_off[6] = {0, 3, 5, 7, 8, 9};
-static __device__ const int op_out[9] = {0, 1, 2, 3, 6, 4, 5, 7, 8};
-static __device__ const int op_w[9] = {1, 1, 1, 1, 1, 1, 1, 1, 1};
-static __device__ const int op_b[9] = {0, 0, 0, 0, 0, 0, 1, 2, 3};
-static __device__ const int op_e[9] = {0, 0, 0, 0, 0, 1, 2, 3, 5};
-static __device__ const int op_kind[9] = {1, 0, 0, 2, 2, 1, 0, 2, 1};
-static __device__ const int op_dg[9] = {0, 0, 0, 0, 0, 0, 0, 4, 0};
-static __device__ const int2 prod[5] = {{3, 1}, {3, 2}, {6, 1}, {6, 2}, {7, 5}};
-constexpr int F_LEVELS = 3;
-constexpr int B_LEVELS = 3;
-static __device__ const int f_rows[3] = {0, 1, 2};
-static __device__ const int f_lev_off[4] = {0, 1, 2, 3};
-static __device__ const int b_rows[3] = {2, 1, 0};
-static __device__ const int b_lev_off[4] = {0, 1, 2, 3};
-static __device__ const int lo_off[4] = {0, 0, 1, 3};
-static __device__ const int2 lo[3] = {{3, 0}, {6, 0}, {7, 1}};
-static __device__ const int up_off[4] = {0, 2, 3, 3};
-static __device__ const int2 up[3] = {{1, 1}, {2, 2}, {5, 2}};
+constexpr int N_LU_ZERO = 0;
+static __device__ const int lu_zero[1] = {0};
+constexpr int LU_STEPS = 7;
+constexpr int SV_STEPS = 8;
+static __device__ const unsigned long long lu_fs[224] = {
+    0x3000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000000000003ull, 0x2000000000006ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000100030004ull, 0x1000200030005ull, 0x1000100060007ull, 0x1000200060008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x3000000000004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000400000007ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000500070008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x3000000000008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+};
+static __device__ const unsigned long long sv_fs[256] = {
+    0x1000000030001ull, 0x1000000060002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000100070002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000800000002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000200050001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000400000001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000100010000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000200020000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+};
 static __device__ const int diag[3] = {0, 4, 8};
 }  // namespace coop
 
@@ -276,7 +325,7 @@ struct Mech {
     return fmax(0.2, fmin(fac, 6.0));
   }
 
-  // ---- warp-cooperative attempt (tables + level schedules) ----
+  // ---- warp-cooperative attempt (tables + static warp schedules) ----
   static constexpr int NPART = 6;
   static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
   static constexpr int D = NSLOTS + 4;     // partial derivatives
@@ -304,31 +353,45 @@ struct Mech {
     __syncwarp();
   }
 
-  // Solve (LU) x = b in place on S[base..] by dependency levels.
+  // Run a static warp schedule (emitter/warp_schedule.py) on S: one
+  // multiply-add, pivot multiply or reciprocal per lane and step, a warp
+  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by
+  // base.  The next two steps' words are in flight while one executes.
+  // Returns false if a reciprocal met a zero pivot.
+  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,
+                                                     int steps, int base, unsigned lane) {
+    bool ok = true;
+    unsigned long long cur = __ldg(T + lane);
+    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;
+    for (int s = 0; s < steps; ++s) {
+      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;
+      const int kind = (int)(cur >> 48) & 3;
+      if (kind != 0) {
+        const int out = (int)(cur & 0xffffu) + base;
+        const int ia = (int)((cur >> 16) & 0xffffu);
+        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);
+        const double vo = S[out];
+        if (kind == 3) {
+          ok = ok && (vo != 0.0);
+          S[out] = 1.0 / vo;
+        } else {
+          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.
+          const double vb = S[ib];
+          const double x = kind == 1 ? -S[ia] : vo;
+          const double z = kind == 1 ? vo : -0.0;
+          S[out] = fma(x, vb, z);
+        }
+      }
+      __syncwarp();
+      cur = nxt;
+      nxt = nn;
+    }
+    return ok;
+  }
+
+  // Solve (LU) x = b in place on S[base..].
   __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {
-    namespace T = coop;
-    for (int l = 0; l < T::F_LEVELS; ++l) {
-      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {
-        const int i = T::f_rows[j];
-        double v = S[base + i];
-        const int e1 = T::lo_off[i + 1];
-        #pragma unroll 4
-        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }
-        S[base + i] = v;
-      }
-      __syncwarp();
-    }
-    for (int l = 0; l < T::B_LEVELS; ++l) {
-      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {
-        const int i = T::b_rows[j];
-        double v = S[base + i];
-        const int e1 = T::up_off[i + 1];
-        #pragma unroll 4
-        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }
-        S[base + i] = v * S[T::diag[i]];
-      }
-      __syncwarp();
-    }
+    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);
   }
 
   // One attempt by a whole warp on the cell held in shared memory S
@@ -349,6 +412,7 @@ struct Mech {
       S[D + p] = d;
     }
     __syncwarp();
+    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;
     for (int w = lane; w < T::NW; w += 32) {
       bool first = !T::w_diag[w];
       double v = T::w_diag[w] ? inv_g_dt : 0.0;
@@ -359,22 +423,8 @@ struct Mech {
       S[T::w_slot[w]] = v;
     }
     __syncwarp();
-    // LU by dependency levels.
-    bool ok = true;
-    for (int l = 0; l < T::LU_LEVELS; ++l) {
-      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {
-        const int out = T::op_out[j];
-        double v = T::op_w[j] ? S[out] : 0.0;
-        const int q1 = T::op_e[j];
-        #pragma unroll 4
-        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }
-        const int kind = T::op_kind[j];
-        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }
-        else if (kind == 2) S[out] = v * S[T::op_dg[j]];
-        else S[out] = v;
-      }
-      __syncwarp();
-    }
+    // LU by the static warp schedule (fill-in slots were zeroed with W).
+    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);
     if (__any_sync(0xffffffffu, !ok)) status |= 1;
     fun_coop(S, S + Y, k, lane);
     for (int i = lane; i < NV; i += 32) S[12 + i] = S[F + i];

@@ -21,26 +21,143 @@ static __device__ const int w_diag[26] = {1, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0,
 static __device__ const int w_off[27] = {0, 2, 4, 5, 8, 10, 12, 14, 15, 18, 20, 25, 26, 27, 28, 30, 31, 36, 37, 38, 39, 40, 42, 43, 44, 45, 47};
 static __device__ const int w_p[47] = {7, 8, 6, 9, 7, 1, 4, 13, 0, 2, 3, 5, 12, 14, 8, 1, 4, 13, 0, 2, 3, 5, 6, 9, 11, 10, 12, 8, 1, 4, 2, 3, 5, 6, 9, 11, 10, 13, 11, 10, 12, 14, 13, 11, 10, 12, 14};
 static __device__ const double w_c[47] = {1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, -2.0, 1.0, -1.0, 1.0, 1.0, -1.0, -2.0, 1.0, -2.0, -1.0, 1.0, 1.0, -1.0, -2.0, -1.0, -2.0, -1.0, -1.0, -1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, -1.0, 1.0, 1.0, -1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 1.0};
-constexpr int LU_LEVELS = 9;
 constexpr int NW = 26;
-static __device__ const int lu_lev_off[10] = {0, 6, 13, 16, 20, 23, 25, 27, 28, 29};
-static __device__ const int op_out[29] = {0, 1, 3, 4, 6, 11, 2, 7, 13, 8, 14, 19, 24, 5, 9, 12, 10, 15, 20, 25, 16, 18, 17, 21, 26, 23, 22, 27, 28};
-static __device__ const int op_w[29] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 1, 0, 1, 1, 1, 1, 1, 1, 1};
-static __device__ const int op_b[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 0, 1, 4, 2, 5, 6, 7, 8, 12, 11, 14, 16, 20, 18, 23, 25};
-static __device__ const int op_e[29] = {0, 0, 0, 0, 1, 4, 0, 0, 0, 1, 1, 1, 1, 1, 2, 5, 4, 6, 7, 8, 11, 14, 12, 16, 18, 23, 20, 25, 29};
-static __device__ const int op_kind[29] = {1, 0, 1, 0, 0, 0, 2, 2, 2, 2, 2, 2, 2, 0, 1, 0, 0, 2, 2, 2, 1, 0, 0, 2, 2, 0, 1, 2, 1};
-static __device__ const int op_dg[29] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 3, 3, 3, 3, 0, 0, 0, 0, 9, 9, 9, 0, 0, 0, 16, 16, 0, 0, 22, 0};
-static __device__ const int2 prod[29] = {{2, 1}, {8, 4}, {7, 1}, {8, 5}, {8, 6}, {14, 4}, {19, 4}, {24, 4}, {13, 1}, {14, 5}, {15, 10}, {15, 11}, {14, 6}, {15, 12}, {19, 5}, {20, 10}, {24, 5}, {25, 10}, {20, 11}, {21, 17}, {19, 6}, {20, 12}, {21, 18}, {25, 11}, {26, 17}, {24, 6}, {25, 12}, {26, 18}, {27, 23}};
-constexpr int F_LEVELS = 6;
-constexpr int B_LEVELS = 5;
-static __device__ const int f_rows[6] = {0, 1, 2, 3, 4, 5};
-static __device__ const int f_lev_off[7] = {0, 1, 2, 3, 4, 5, 6};
-static __device__ const int b_rows[6] = {5, 4, 3, 0, 2, 1};
-static __device__ const int b_lev_off[6] = {0, 1, 2, 3, 5, 6};
-static __device__ const int lo_off[7] = {0, 0, 1, 3, 6, 9, 13};
-static __device__ const int2 lo[13] = {{2, 0}, {7, 0}, {8, 1}, {13, 0}, {14, 1}, {15, 2}, {19, 1}, {20, 2}, {21, 3}, {24, 1}, {25, 2}, {26, 3}, {27, 4}};
-static __device__ const int up_off[7] = {0, 1, 4, 7, 9, 10, 10};
-static __device__ const int2 up[10] = {{1, 3}, {4, 2}, {5, 3}, {6, 5}, {10, 3}, {11, 4}, {12, 5}, {17, 4}, {18, 5}, {23, 5}};
+constexpr int N_LU_ZERO = 3;
+static __device__ const int lu_zero[3] = {20, 25, 18};
+constexpr int LU_STEPS = 13;
+constexpr int SV_STEPS = 19;
+static __device__ const unsigned long long lu_fs[416] = {
+    0x3000000000000ull, 0x3000000000003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000000000002ull, 0x2000000000007ull, 0x200000000000dull, 0x2000300000008ull, 0x200030000000eull, 0x2000300000013ull, 0x2000300000018ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000100020005ull, 0x1000400080009ull, 0x100010007000aull, 0x100060008000cull, 0x10004000e000full, 0x1000400130014ull, 0x1000400180019ull, 0x10001000d0010ull,
+    0x10006000e0012ull, 0x1000600130017ull, 0x100060018001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x3000000000009ull, 0x100050008000aull, 0x10005000e0010ull, 0x1000500130015ull, 0x100050018001aull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x200090000000full, 0x2000900000014ull, 0x2000900000019ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000a000f0010ull, 0x1000b000f0011ull, 0x1000c000f0012ull, 0x1000a00140015ull, 0x1000a0019001aull, 0x1000b00140016ull, 0x1000c00140017ull, 0x1000b0019001bull,
+    0x1000c0019001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x3000000000010ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2001000000015ull, 0x200100000001aull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1001100150016ull, 0x1001200150017ull, 0x10011001a001bull, 0x10012001a001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x3000000000016ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x200160000001bull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10017001b001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x300000000001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+};
+static __device__ const unsigned long long sv_fs[608] = {
+    0x1000000020001ull, 0x1000000070002ull, 0x10000000d0003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000100080002ull, 0x10001000e0003ull, 0x1000100130004ull, 0x1000100180005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10002000f0003ull, 0x1000200140004ull, 0x1000200190005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000300150004ull, 0x10003001a0005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10004001b0005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2001c00000005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000500170004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2001600000004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000400110003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000500120003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2001000000003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10003000a0002ull, 0x1000300010000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10004000b0002ull, 0x2000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x10005000c0002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000900000002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000200040001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000300050001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x1000500060001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x2000300000001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+};
 static __device__ const int diag[6] = {0, 3, 9, 16, 22, 28};
 }  // namespace coop
 
@@ -429,7 +546,7 @@ struct Mech {
     return fmax(0.2, fmin(fac, 6.0));
   }
 
-  // ---- warp-cooperative attempt (tables + level schedules) ----
+  // ---- warp-cooperative attempt (tables + static warp schedules) ----
   static constexpr int NPART = 15;
   static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
   static constexpr int D = NSLOTS + 10;     // partial derivatives
@@ -457,31 +574,45 @@ struct Mech {
     __syncwarp();
   }
 
-  // Solve (LU) x = b in place on S[base..] by dependency levels.
+  // Run a static warp schedule (emitter/warp_schedule.py) on S: one
+  // multiply-add, pivot multiply or reciprocal per lane and step, a warp
+  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by
+  // base.  The next two steps' words are in flight while one executes.
+  // Returns false if a reciprocal met a zero pivot.
+  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,
+                                                     int steps, int base, unsigned lane) {
+    bool ok = true;
+    unsigned long long cur = __ldg(T + lane);
+    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;
+    for (int s = 0; s < steps; ++s) {
+      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;
+      const int kind = (int)(cur >> 48) & 3;
+      if (kind != 0) {
+        const int out = (int)(cur & 0xffffu) + base;
+        const int ia = (int)((cur >> 16) & 0xffffu);
+        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);
+        const double vo = S[out];
+        if (kind == 3) {
+          ok = ok && (vo != 0.0);
+          S[out] = 1.0 / vo;
+        } else {
+          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.
+          const double vb = S[ib];
+          const double x = kind == 1 ? -S[ia] : vo;
+          const double z = kind == 1 ? vo : -0.0;
+          S[out] = fma(x, vb, z);
+        }
+      }
+      __syncwarp();
+      cur = nxt;
+      nxt = nn;
+    }
+    return ok;
+  }
+
+  // Solve (LU) x = b in place on S[base..].
   __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {
-    namespace T = coop;
-    for (int l = 0; l < T::F_LEVELS; ++l) {
-      for (int j = T::f_lev_off[l] + lane; j < T::f_lev_off[l + 1]; j += 32) {
-        const int i = T::f_rows[j];
-        double v = S[base + i];
-        const int e1 = T::lo_off[i + 1];
-        #pragma unroll 4
-        for (int e = T::lo_off[i]; e < e1; ++e) { const int2 p = T::lo[e]; v = fma(-S[p.x], S[base + p.y], v); }
-        S[base + i] = v;
-      }
-      __syncwarp();
-    }
-    for (int l = 0; l < T::B_LEVELS; ++l) {
-      for (int j = T::b_lev_off[l] + lane; j < T::b_lev_off[l + 1]; j += 32) {
-        const int i = T::b_rows[j];
-        double v = S[base + i];
-        const int e1 = T::up_off[i + 1];
-        #pragma unroll 4
-        for (int e = T::up_off[i]; e < e1; ++e) { const int2 p = T::up[e]; v = fma(-S[p.x], S[base + p.y], v); }
-        S[base + i] = v * S[T::diag[i]];
-      }
-      __syncwarp();
-    }
+    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);
   }
 
   // One attempt by a whole warp on the cell held in shared memory S
@@ -502,6 +633,7 @@ struct Mech {
       S[D + p] = d;
     }
     __syncwarp();
+    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;
     for (int w = lane; w < T::NW; w += 32) {
       bool first = !T::w_diag[w];
       double v = T::w_diag[w] ? inv_g_dt : 0.0;
@@ -512,22 +644,8 @@ struct Mech {
       S[T::w_slot[w]] = v;
     }
     __syncwarp();
-    // LU by dependency levels.
-    bool ok = true;
-    for (int l = 0; l < T::LU_LEVELS; ++l) {
-      for (int j = T::lu_lev_off[l] + lane; j < T::lu_lev_off[l + 1]; j += 32) {
-        const int out = T::op_out[j];
-        double v = T::op_w[j] ? S[out] : 0.0;
-        const int q1 = T::op_e[j];
-        #pragma unroll 4
-        for (int q = T::op_b[j]; q < q1; ++q) { const int2 p = T::prod[q]; v = fma(-S[p.x], S[p.y], v); }
-        const int kind = T::op_kind[j];
-        if (kind == 1) { ok = ok && (v != 0.0); S[out] = 1.0 / v; }
-        else if (kind == 2) S[out] = v * S[T::op_dg[j]];
-        else S[out] = v;
-      }
-      __syncwarp();
-    }
+    // LU by the static warp schedule (fill-in slots were zeroed with W).
+    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);
     if (__any_sync(0xffffffffu, !ok)) status |= 1;
     fun_coop(S, S + Y, k, lane);
     for (int i = lane; i < NV; i += 32) S[35 + i] = S[F + i];
