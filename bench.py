@@ -295,7 +295,9 @@ def main():
             stream.synchronize()
             kernel_ms.append(ev[0].elapsed_time(ev[1]))
             log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms")
-    # Capture the window (hs rate-constant launches + 1 integrate launch).
+    # Capture the window: hs rate-constant launches, the persistent integrate
+    # launch and, with parking enabled, the cooperative launch (which finds no
+    # parked cell: no cell of a 24-step window reaches 24 x 3000 attempts).
     g = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
         with torch.cuda.graph(g, stream=stream):
@@ -348,10 +350,10 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
-        "gpu_launches": args.steps * (hs + 1),
+        "gpu_launches": args.steps * (hs + 1 + (int(os.environ.get("MKPP_DEFER_AFTER", "3000")) > 0)),
         "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
-                   "defer_after": os.environ.get("MKPP_DEFER_AFTER", "0"), "cost_order": bool(args.order),
+                   "defer_after_per_host_step": os.environ.get("MKPP_DEFER_AFTER", "3000"), "cost_order": bool(args.order),
                    "max_attempts_per_call": args.max_attempts},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],

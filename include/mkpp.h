@@ -112,9 +112,11 @@ size_t mkpp_gpu_workspace_bytes(size_t num_cells);
 /* Process-wide launch tuning of the integrate kernels (the autotuner's
  * knobs): register_variant 2 (up to 255 registers per thread) or 4 (up to
  * 128, more resident warps), 0 keeps the current one; blocks_per_sm caps the
- * resident blocks per SM (0: as many as fit); defer_after: attempts of one cell
- * (over all its host steps) after which the persistent kernel hands it to the
- * warp-cooperative kernel (0: never, -1 keeps the current value). */
+ * resident blocks per SM (0: as many as fit); defer_after: attempts per host
+ * step of a launch (a launch over S steps: defer_after * S in all) after which
+ * the persistent kernel hands a cell to the warp-cooperative kernel (0: never,
+ * -1 keeps the current value; default 3000, environment MKPP_DEFER_AFTER).
+ * Results do not depend on it: a handed-off cell ends bit-identical. */
 int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after);
 
 /* Rate constants of every reaction into ktab[cell + num_cells * reaction].

@@ -83,18 +83,25 @@ int device_fail(mkpp_handle_s* h, cudaError_t err, const char* what) {
 //  register_variant  launch-bounds minimum of resident blocks (2: up to 255
 //                    registers per thread, 4: up to 128, more resident warps);
 //  blocks_per_sm     cap on resident blocks per SM (0: as many as fit);
-//  defer_after       attempts of one cell (all host steps) after which the
-//                    persistent kernel parks it for the warp-cooperative
-//                    kernel (0: never, the default).  On GB300 a warp FP64
-//                    instruction costs the same pipe time with one active lane
-//                    as with 32, and the sparse LU keeps few lanes busy, so
-//                    the cooperative form does not beat one lane per cell.
+//  defer_after       attempts per host step of the launch after which the
+//                    persistent kernel parks a cell for the warp-cooperative
+//                    kernel (0: never).  A launch over S host steps parks a
+//                    cell after defer_after * S attempts in all.  A
+//                    cooperative SAPRC99 attempt takes ~0.37 ms against
+//                    ~1 ms on one lane, but the cooperative kernel has about
+//                    a fifth of the lanes' throughput, so only the tail
+//                    should park.  The default, 3000, parks ~7% of the cells
+//                    in the stiff first host step of the SAPRC99 workload,
+//                    ~0.15% (its slowest cells) in the later ones, and none
+//                    in a 24-step window (whose slowest cell needs ~22000).
 // Initial values come from MKPP_REGISTER_VARIANT, MKPP_BLOCKS_PER_SM and
 // MKPP_DEFER_AFTER, and mkpp_set_launch_tuning changes them.
+constexpr int kDefaultDeferPerStep = 3000;
+
 struct Tuning {
   int register_variant = 2;
   int blocks_per_sm = 0;
-  int defer_after = 0;
+  int defer_after = kDefaultDeferPerStep;
 };
 
 Tuning& tuning() {
@@ -183,7 +190,8 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   const LaunchConfig& cfg = launch_config();
   if (cudaMemsetAsync(ws, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
   if (mode == 1) {
-    a.defer_after = tuning().defer_after;
+    const long long park = (long long)tuning().defer_after * std::max(1, a.steps);
+    a.defer_after = (int)std::min<long long>(park, INT32_MAX);
     a.defer = a.defer_after > 0 ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
     if (!a.defer) a.defer_after = 0;
     if (cfg.minb == 4) {

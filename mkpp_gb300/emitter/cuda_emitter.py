@@ -153,251 +153,249 @@ def _c_u64_array(c, name, values):
 
 
 def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None):
-    """Warp-cooperative form of one attempt: the same arithmetic, element by
-    element, as ``attempt`` (same operand order in every sum and product), with
-    the independent elements of each phase spread over the 32 lanes of a warp.
-    Used for the few cells whose step count makes one lane too slow."""
+    """Warp-cooperative form of one attempt: the same arithmetic, operation by
+    operation, as ``attempt``, with each tableau stage run as a static 32-lane
+    schedule (``warp_schedule``).  Used for the few cells whose step count
+    makes one lane too slow."""
     v2l = plan.phys_to_var
     nr = len(plan.reactions)
-    # --- rates q_r = k_r * y ... (factor order of fun)
-    r_off, r_y = [0], []
-    for r in plan.reactions:
-        for s_, pw in r.reactants:
-            r_y += [v2l[s_]] * pw
-        r_off.append(len(r_y))
-    # --- F_i = sum over reactions (order of fun)
-    f_off, f_r, f_c = [0], [], []
-    contrib = {i: [] for i in range(nv)}
-    for r in plan.reactions:
-        for s_, coef in r.net:
-            contrib[v2l[s_]].append((coef, r.index))
-    for i in range(nv):
-        for coef, ri in contrib[i]:
-            f_r.append(ri)
-            f_c.append(_lit(coef))
-        f_off.append(len(f_r))
-    # --- partials d = k * [pw] * y ... (factor order of jac_w); factor -1 = the literal pw
-    d_r, d_off, d_fac, d_lit = [], [0], [], []
-    pidx = {}
-    for r in plan.reactions:
-        terms = list(r.reactants)
-        for idx, (s_, pw) in enumerate(terms):
-            fac = []
-            lit = 1.0
-            for jdx, (s2, pw2) in enumerate(terms):
-                if jdx == idx:
-                    if pw2 > 1:
-                        fac.append(-1)
-                        lit = float(pw2)
-                        fac += [v2l[s2]] * (pw2 - 1)
-                else:
-                    fac += [v2l[s2]] * pw2
-            pidx[(r.index, s_)] = len(d_r)
-            d_r.append(r.index)
-            d_fac += fac
-            d_lit.append(_lit(lit))
-            d_off.append(len(d_fac))
-    npart = len(d_r)
-    # --- W slots: init (diag) + terms (coef, partial) in jac_w order
-    w_slot, w_diag, w_off, w_p, w_c = [], [], [0], [], []
-    wterms = {loc: [] for loc in plan.w_slots}
-    for r in plan.reactions:
-        for s_, coef in r.net:
-            for s2, _pw in r.reactants:
-                wterms[(v2l[s_], v2l[s2])].append((-coef, pidx[(r.index, s2)]))
-    for loc in plan.w_slots:
-        w_slot.append(plan.lu_index[loc])
-        w_diag.append(int(loc[0] == loc[1]))
-        for coef, pi in wterms[loc]:
-            w_p.append(pi)
-            w_c.append(_lit(coef))
-        w_off.append(len(w_p))
-    # --- LU and solves: static 32-lane schedules of single multiply-adds
-    lu_prog = warp_schedule.lu_program(plan)
-    lu_steps = warp_schedule.schedule(lu_prog)
-    sv_prog = warp_schedule.solve_program(plan)
-    sv_steps = warp_schedule.schedule(sv_prog, relative=True)
-    lu_zero = warp_schedule.lu_zero_slots(plan)
-    c("")
-    c("  // ---- warp-cooperative attempt (tables + static warp schedules) ----")
-    c(f"  static constexpr int NPART = {npart};")
     nq = max(nr, nv)
-    c(f"  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm")
-    c(f"  static constexpr int D = NSLOTS + {nq};     // partial derivatives")
-    c(f"  static constexpr int COOP_SLOTS = NSLOTS + {nq} + NPART;")
-    t = _Code()
-    t("// Tables of the warp-cooperative attempt (device constant data).")
-    t("namespace coop {")
-    c_ = c
-    c = t
-    _c_array(c, "int", "r_off", r_off)
-    _c_array(c, "int", "r_y", r_y)
-    _c_array(c, "int", "f_off", f_off)
-    _c_array(c, "int", "f_r", f_r)
-    _c_array(c, "double", "f_c", f_c)
-    _c_array(c, "int", "d_r", d_r)
-    _c_array(c, "int", "d_off", d_off)
-    _c_array(c, "int", "d_fac", d_fac)
-    _c_array(c, "double", "d_lit", d_lit)
-    _c_array(c, "int", "w_slot", w_slot)
-    _c_array(c, "int", "w_diag", w_diag)
-    _c_array(c, "int", "w_off", w_off)
-    _c_array(c, "int", "w_p", w_p)
-    _c_array(c, "double", "w_c", w_c)
-    c(f"constexpr int NW = {len(w_slot)};")
-    c(f"constexpr int N_LU_ZERO = {len(lu_zero)};")
-    _c_array(c, "int", "lu_zero", lu_zero)
-    c(f"constexpr int LU_STEPS = {len(lu_steps)};")
-    c(f"constexpr int SV_STEPS = {len(sv_steps)};")
-    _c_u64_array(c, "lu_fs", warp_schedule.encode(lu_prog, lu_steps))
-    _c_u64_array(c, "sv_fs", warp_schedule.encode(sv_prog, sv_steps))
-    _c_array(c, "int", "diag", plan.diag)
-    c("}  // namespace coop")
-    c("")
-    c = c_
-    plan._coop_tables = t.text()
-    # accumulate like _accumulate: first term c=1 -> t, c=-1 -> -t, else c*t; then +,-,fma
-    c("  __device__ __forceinline__ static double acc_term(bool first, double acc, double coef, double t) {")
-    c("    if (first) return coef == 1.0 ? t : (coef == -1.0 ? -t : coef * t);")
-    c("    return coef == 1.0 ? acc + t : (coef == -1.0 ? acc - t : fma(coef, t, acc));")
-    c("  }")
-    c("")
-    c("  // F(y) into S[F..] for the state yv (S[Y..] or the stage state), cooperatively.")
-    c("  template <class KA>")
-    c("  __device__ __forceinline__ static void fun_coop(double* S, const double* yv, const KA& k, unsigned lane) {")
-    c("    namespace T = coop;")
-    c("    for (int r = lane; r < NR; r += 32) {")
-    c("      double q = k(r);")
-    c("      for (int e = T::r_off[r]; e < T::r_off[r + 1]; ++e) q = q * yv[T::r_y[e]];")
-    c("      S[Q + r] = q;")
-    c("    }")
-    c("    __syncwarp();")
-    c("    for (int i = lane; i < NV; i += 32) {")
-    c("      double v = 0.0;")
-    c("      for (int e = T::f_off[i]; e < T::f_off[i + 1]; ++e) v = acc_term(e == T::f_off[i], v, T::f_c[e], S[Q + T::f_r[e]]);")
-    c("      S[F + i] = v;")
-    c("    }")
-    c("    __syncwarp();")
-    c("  }")
-    c("")
-    c("  // Run a static warp schedule (emitter/warp_schedule.py) on S: one")
-    c("  // multiply-add, pivot multiply or reciprocal per lane and step, a warp")
-    c("  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by")
-    c("  // base.  The next two steps' words are in flight while one executes.")
-    c("  // Returns false if a reciprocal met a zero pivot.")
-    c("  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,")
-    c("                                                     int steps, int base, unsigned lane) {")
-    c("    bool ok = true;")
-    c("    unsigned long long cur = __ldg(T + lane);")
-    c("    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;")
-    c("    for (int s = 0; s < steps; ++s) {")
-    c("      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;")
-    c("      const int kind = (int)(cur >> 48) & 3;")
-    c("      if (kind != 0) {")
-    c("        const int out = (int)(cur & 0xffffu) + base;")
-    c("        const int ia = (int)((cur >> 16) & 0xffffu);")
-    c("        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);")
-    c("        const double vo = S[out];")
-    c("        if (kind == 3) {")
-    c("          ok = ok && (vo != 0.0);")
-    c("          S[out] = 1.0 / vo;")
-    c("        } else {")
-    c("          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.")
-    c("          const double vb = S[ib];")
-    c("          const double x = kind == 1 ? -S[ia] : vo;")
-    c("          const double z = kind == 1 ? vo : -0.0;")
-    c("          S[out] = fma(x, vb, z);")
-    c("        }")
-    c("      }")
-    c("      __syncwarp();")
-    c("      cur = nxt;")
-    c("      nxt = nn;")
-    c("    }")
-    c("    return ok;")
-    c("  }")
-    c("")
-    c("  // Solve (LU) x = b in place on S[base..].")
-    c("  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {")
-    c("    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);")
-    c("  }")
-    c("")
-    c("  // One attempt by a whole warp on the cell held in shared memory S")
-    c("  // (NSLOTS + NR + NPART doubles).  Same values as attempt(); the error norm")
-    c("  // is summed by lane 0 in species order.  Returns err on every lane.")
-    c("  template <class KA>")
-    c("  __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,")
-    c("                                                       unsigned lane) {")
-    c("    namespace T = coop;")
-    c("    const double inv_g_dt = 1.0 / (GAMMA * h);")
-    c("    // Jacobian partials, then W into the LU slots.")
-    c("    for (int p = lane; p < NPART; p += 32) {")
-    c("      double d = k(T::d_r[p]);")
-    c("      for (int e = T::d_off[p]; e < T::d_off[p + 1]; ++e) {")
-    c("        const int f = T::d_fac[e];")
-    c("        d = d * (f < 0 ? T::d_lit[p] : S[Y + f]);")
-    c("      }")
-    c("      S[D + p] = d;")
-    c("    }")
-    c("    __syncwarp();")
-    c("    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;")
-    c("    for (int w = lane; w < T::NW; w += 32) {")
-    c("      bool first = !T::w_diag[w];")
-    c("      double v = T::w_diag[w] ? inv_g_dt : 0.0;")
-    c("      for (int e = T::w_off[w]; e < T::w_off[w + 1]; ++e) {")
-    c("        v = acc_term(first, v, T::w_c[e], S[D + T::w_p[e]]);")
-    c("        first = false;")
-    c("      }")
-    c("      S[T::w_slot[w]] = v;")
-    c("    }")
-    c("    __syncwarp();")
-    c("    // LU by the static warp schedule (fill-in slots were zeroed with W).")
-    c("    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);")
-    c("    if (__any_sync(0xffffffffu, !ok)) status |= 1;")
-    cur_f = None
+    npart = sum(len(r.reactants) for r in plan.reactions)
+    Q = nslots                      # rates q_r (then q_i of the error norm)
+    D = nslots + nq                 # Jacobian partial derivatives
+    CB = D + npart                  # constants: -0, +0, 1, 1/(gamma h), c_ij/h, literals
+    ZN, ZP, ONE, IG = CB, CB + 1, CB + 2, CB + 3
+    cterm_slot = {}
+    for st in range(2, stages + 1):
+        for j in range(1, st):
+            cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+            if cv != 0.0:
+                cterm_slot[(st, j)] = CB + 4 + len(cterm_slot)
+    literals: dict[float, int] = {}
+    lit_base = CB + 4 + len(cterm_slot)
+
+    def lit(v):
+        v = float(v)
+        if v not in literals:
+            literals[v] = lit_base + len(literals)
+        return literals[v]
+
+    def program():
+        return warp_schedule.Program(ZN, ZP, ONE, lit)
+
+    def fun(P, yv):
+        """F(y) into S[FS..] for y in S[yv..]: rates q_r = k_r * y ... in
+        reactant order, then F_i as the sum over reactions in reaction order."""
+        for r in plan.reactions:
+            fac = [v2l[s_] for s_, pw in r.reactants for _ in range(pw)]
+            if not fac:
+                P.copy(Q + r.index, Mech_KT + r.index)
+            for n_, f in enumerate(fac):
+                P.mul(Q + r.index, (Mech_KT + r.index) if n_ == 0 else Q + r.index, yv + f)
+        contrib = {i: [] for i in range(nv)}
+        for r in plan.reactions:
+            for s_, coef in r.net:
+                contrib[v2l[s_]].append((coef, r.index))
+        for i in range(nv):
+            if not contrib[i]:
+                P.zero(FS + i)
+            for n_, (coef, ri) in enumerate(contrib[i]):
+                P.acc_term(FS + i, n_ == 0, float(coef), Q + ri)
+
+    def jac_w(P):
+        """Partials d = k [* power] * y ... at S[Y..], then W = I/(gamma h) - J
+        into the LU slots, and the fill-in slots zeroed."""
+        pidx = {}
+        p = 0
+        for r in plan.reactions:
+            terms = list(r.reactants)
+            for idx, (s_, pw) in enumerate(terms):
+                fac = []
+                for jdx, (s2, pw2) in enumerate(terms):
+                    if jdx == idx:
+                        if pw2 > 1:
+                            fac.append(lit(float(pw2)))
+                            fac += [Y + v2l[s2]] * (pw2 - 1)
+                    else:
+                        fac += [Y + v2l[s2]] * pw2
+                if not fac:
+                    P.copy(D + p, Mech_KT + r.index)
+                for n_, f in enumerate(fac):
+                    P.mul(D + p, (Mech_KT + r.index) if n_ == 0 else D + p, f)
+                pidx[(r.index, s_)] = p
+                p += 1
+        wterms = {loc: [] for loc in plan.w_slots}
+        for r in plan.reactions:
+            for s_, coef in r.net:
+                for s2, _pw in r.reactants:
+                    wterms[(v2l[s_], v2l[s2])].append((-coef, pidx[(r.index, s2)]))
+        for loc in plan.w_slots:
+            out = plan.lu_index[loc]
+            terms = wterms[loc]
+            if loc[0] == loc[1]:
+                if not terms:
+                    P.copy(out, IG)
+                for n_, (coef, pi) in enumerate(terms):
+                    P.acc_term(out, False, float(coef), D + pi, acc=IG if n_ == 0 else None)
+            else:
+                if not terms:
+                    P.zero(out)
+                for n_, (coef, pi) in enumerate(terms):
+                    P.acc_term(out, n_ == 0, float(coef), D + pi)
+        for sl in warp_schedule.lu_zero_slots(plan):
+            P.zero(sl)
+
+    # The rate constants of the host step sit in the KT slots (after the stage
+    # vectors, F and the increment): KT = DY + NV.
+    Mech_KT = DY + nv
+    progs = []
     for st in range(1, stages + 1):
+        P = program()
         kb = K0 + (st - 1) * nv
+        if st == 1:
+            jac_w(P)
+            P.lu(plan)
         if NewF[st - 1]:
             if st == 1:
-                c("    fun_coop(S, S + Y, k, lane);")
+                fun(P, Y)
             else:
+                # Stage state Y + sum a_j K_j into the DY slots; Q holds a*K
+                # partial terms (rates are written after the state is read).
                 terms = []
                 for j in range(1, st):
                     a = A[(st - 1) * (st - 2) // 2 + j - 1]
                     if a != 0.0:
                         terms.append((a, j))
-                expr = "S[Y + i]"
-                for a, j in terms:
-                    kk = f"S[{K0 + (j - 1) * nv} + i]"
-                    expr = f"{expr} + {kk}" if a == 1.0 else f"{expr} + {_lit(a)} * {kk}"
-                c("    // Stage state into the DY slots (free until the error block).")
-                c(f"    for (int i = lane; i < NV; i += 32) S[DY + i] = {expr};")
-                c("    __syncwarp();")
-                c("    fun_coop(S, S + DY, k, lane);")
-        cterms = []
-        if st > 1:
+                for i in range(nv):
+                    acc = Y + i
+                    for a, j in terms:
+                        kk = K0 + (j - 1) * nv + i
+                        if a == 1.0:
+                            P.fma(DY + i, kk, ONE, acc)
+                        else:
+                            P.mul(Q + i, kk, lit(a))
+                            P.fma(DY + i, Q + i, ONE, acc)
+                        acc = DY + i
+                    if not terms:
+                        P.copy(DY + i, Y + i)
+                fun(P, DY)
+        for i in range(nv):
+            P.copy(kb + i, FS + i)
             for j in range(1, st):
-                cv = C[(st - 1) * (st - 2) // 2 + j - 1]
-                if cv != 0.0:
-                    cterms.append((cv, j))
-        for cv, j in cterms:
-            c(f"    const double c{st}{j} = {_lit(cv)} / h;")
-        expr = "S[F + i]"
-        for cv, j in cterms:
-            expr = f"fma(c{st}{j}, S[{K0 + (j - 1) * nv} + i], {expr})"
-        c(f"    for (int i = lane; i < NV; i += 32) S[{kb} + i] = {expr};")
-        c("    __syncwarp();")
-        c(f"    solve_coop(S, {kb}, lane);")
+                if (st, j) in cterm_slot:
+                    P.fma(kb + i, cterm_slot[(st, j)], K0 + (j - 1) * nv + i, kb + i)
+        P.solve(plan, kb)
+        progs.append(P.ops)
+    sched = [warp_schedule.schedule(ops) for ops in progs]
+    nconst = 4 + len(cterm_slot) + len(literals)
+    const_vals = ["-0.0", "0.0", "1.0", "0.0"] + ["0.0"] * len(cterm_slot) + [_lit(v) for v in literals]
+
+    c("")
+    c("  // ---- warp-cooperative attempt (static warp schedules) ----")
+    c(f"  static constexpr int NPART = {npart};")
+    c(f"  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm")
+    c(f"  static constexpr int D = NSLOTS + {nq};     // partial derivatives")
+    c(f"  static constexpr int CB = D + NPART;        // constants")
+    c(f"  static constexpr int NCONST = {nconst};")
+    c(f"  static constexpr int COOP_SLOTS = CB + NCONST;")
+    t = _Code()
+    t("// Tables of the warp-cooperative attempt (device constant data).")
+    t("namespace coop {")
+    t(f"static __device__ const double const_val[{nconst}] = {{{', '.join(const_vals)}}};")
+    offs = [0]
+    for st_ in sched:
+        offs.append(offs[-1] + len(st_))
+    t(f"static __device__ const int stage_step[{len(offs)}] = {{{', '.join(map(str, offs))}}};")
+    words = []
+    for ops, st_ in zip(progs, sched):
+        words += warp_schedule.encode(ops, st_)
+    _c_u64_array(t, "sched", words)
+    t("}  // namespace coop")
+    t("")
+    plan._coop_tables = t.text()
+    plan._coop_programs = (progs, sched, {"CB": CB, "nconst": nconst, "literals": dict(literals),
+                                          "cterm_slot": dict(cterm_slot), "Y": Y, "K0": K0, "FS": FS,
+                                          "DY": DY, "KT": Mech_KT, "C": list(C), "slots": CB + nconst})
+    c("  // Run steps [s_begin, s_end) of the static warp schedule on S: one")
+    c("  // uniform operation S[out] = fma(+-S[a], S[b], S[c]) (or a pivot")
+    c("  // reciprocal) per lane and step, a warp barrier between steps.  The words")
+    c("  // of the next SCHED_AHEAD steps are in flight while the current ones")
+    c("  // execute; words past the end read as idle lanes.  Returns false if a")
+    c("  // reciprocal met a zero pivot.")
+    c("  static constexpr int SCHED_AHEAD = 8;")
+    c("  __device__ __forceinline__ static bool run_schedule(double* S, int s_begin, int s_end, unsigned lane) {")
+    c("    const unsigned long long* __restrict__ T = coop::sched;")
+    c("    bool ok = true;")
+    c("    unsigned long long cur[SCHED_AHEAD];")
+    c("    #pragma unroll")
+    c("    for (int j = 0; j < SCHED_AHEAD; ++j) {")
+    c("      const int s = s_begin + j;")
+    c("      cur[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;")
+    c("    }")
+    c("    for (int s0 = s_begin; s0 < s_end; s0 += SCHED_AHEAD) {")
+    c("      unsigned long long nxt[SCHED_AHEAD];")
+    c("      #pragma unroll")
+    c("      for (int j = 0; j < SCHED_AHEAD; ++j) {")
+    c("        const int s = s0 + SCHED_AHEAD + j;")
+    c("        nxt[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;")
+    c("      }")
+    c("      #pragma unroll")
+    c("      for (int j = 0; j < SCHED_AHEAD; ++j) {")
+    c("        const unsigned long long w = cur[j];")
+    c("        const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);")
+    c("        const unsigned out = lo & 0xffffu;")
+    c("        if (out != 0xffffu) {")
+    c("          if (hi >> 31) {")
+    c("            const double v = S[out];")
+    c("            ok = ok && (v != 0.0);")
+    c("            S[out] = 1.0 / v;")
+    c("          } else {")
+    c("            // Negation flips the sign bit: exact, like -x in the per-thread code.")
+    c("            const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^")
+    c("                                                  ((long long)(lo >> 31) << 63));")
+    c("            S[out] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
+    c("          }")
+    c("        }")
+    c("        __syncwarp();")
+    c("      }")
+    c("      #pragma unroll")
+    c("      for (int j = 0; j < SCHED_AHEAD; ++j) cur[j] = nxt[j];")
+    c("    }")
+    c("    return ok;")
+    c("  }")
+    c("")
+    c("  // One attempt by a whole warp on the cell held in shared memory S")
+    c("  // (COOP_SLOTS doubles; the rate constants in the KT slots).  Same values")
+    c("  // as attempt(); the error norm is summed by lane 0 in species order.")
+    c("  // Returns err on every lane.")
+    c("  template <class KA>")
+    c("  __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,")
+    c("                                                       unsigned lane) {")
+    c("    (void)k;")
+    c("    namespace T = coop;")
+    c("    for (int i = lane; i < NCONST; i += 32) S[CB + i] = T::const_val[i];")
+    c("    __syncwarp();")
+    c("    if (lane == 0) {")
+    c("      S[CB + 3] = 1.0 / (GAMMA * h);")
+    for (st, j), slot in cterm_slot.items():
+        cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+        c(f"      S[{slot}] = {_lit(cv)} / h;    // c{st}{j} / h")
+    c("    }")
+    c("    __syncwarp();")
+    c("    bool ok = true;")
+    c("    for (int st = 0; st < NSTAGE; ++st) ok = run_schedule(S, T::stage_step[st], T::stage_step[st + 1], lane) && ok;")
+    c("    if (__any_sync(0xffffffffu, !ok)) status |= 1;")
     mterms = [(M[j], j) for j in range(stages) if M[j] != 0.0]
     eterms = [(E[j], j) for j in range(stages) if E[j] != 0.0]
 
     def lin(terms):
         expr = None
         for cv, j in terms:
-            t = f"k{j}"
+            t_ = f"k{j}"
             if expr is None:
-                expr = t if cv == 1.0 else f"{_lit(cv)} * {t}"
+                expr = t_ if cv == 1.0 else f"{_lit(cv)} * {t_}"
             else:
-                expr = f"{expr} + {t}" if cv == 1.0 else f"fma({_lit(cv)}, {t}, {expr})"
+                expr = f"{expr} + {t_}" if cv == 1.0 else f"fma({_lit(cv)}, {t_}, {expr})"
         return expr or "0.0"
     c("    // Increment, and q_i^2 of the error norm into the rate slots.")
     c("    for (int i = lane; i < NV; i += 32) {")

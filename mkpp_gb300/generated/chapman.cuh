@@ -7,90 +7,182 @@ namespace mkpp_chapman {
 
 // Tables of the warp-cooperative attempt (device constant data).
 namespace coop {
-static __device__ const int r_off[5] = {0, 1, 3, 4, 6};
-static __device__ const int r_y[6] = {2, 1, 2, 0, 1, 0};
-static __device__ const int f_off[4] = {0, 3, 7, 11};
-static __device__ const int f_r[11] = {1, 2, 3, 0, 1, 2, 3, 0, 1, 2, 3};
-static __device__ const double f_c[11] = {1.0, -1.0, -1.0, 2.0, -1.0, 1.0, -1.0, -1.0, -1.0, 1.0, 2.0};
-static __device__ const int d_r[6] = {0, 1, 1, 2, 3, 3};
-static __device__ const int d_off[7] = {0, 0, 1, 2, 2, 3, 4};
-static __device__ const int d_fac[4] = {2, 1, 0, 1};
-static __device__ const double d_lit[6] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
-static __device__ const int w_slot[9] = {0, 1, 2, 3, 4, 5, 6, 7, 8};
-static __device__ const int w_diag[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-static __device__ const int w_off[10] = {0, 2, 4, 5, 7, 9, 11, 13, 15, 17};
-static __device__ const int w_p[17] = {3, 5, 1, 4, 2, 3, 5, 1, 4, 0, 2, 3, 5, 1, 4, 0, 2};
-static __device__ const double w_c[17] = {1.0, 1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 1.0, 1.0, -2.0, 1.0, -1.0, -2.0, 1.0, -2.0, 1.0, 1.0};
-constexpr int NW = 9;
-constexpr int N_LU_ZERO = 0;
-static __device__ const int lu_zero[1] = {0};
-constexpr int LU_STEPS = 7;
-constexpr int SV_STEPS = 8;
-static __device__ const unsigned long long lu_fs[224] = {
-    0x3000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000000000003ull, 0x2000000000006ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000100030004ull, 0x1000200030005ull, 0x1000100060007ull, 0x1000200060008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x3000000000004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000400000007ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000500070008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x3000000000008ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+static __device__ const double const_val[9] = {-0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, -2.0, 2.0};
+static __device__ const int stage_step[4] = {0, 16, 32, 43};
+static __device__ const unsigned long long sched[1376] = {
+    0x29002b001b0023ull, 0x29000b001c0024ull, 0x29000a001c0025ull, 0x29002b001d0026ull, 0x290009001e0027ull, 0x29000a001e0028ull, 0x29000b001b001full, 0x29000a001c0020ull,
+    0x290009001d0021ull, 0x29000a001e0022ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2c002b00260000ull, 0x29002b80240001ull, 0x29002b80250002ull, 0x29002b80260003ull, 0x2c002b00240004ull, 0x29003000230005ull, 0x29002b80260006ull, 0x29002b00240007ull,
+    0x2c002b00230008ull, 0x29000b00200020ull, 0x29000900220022ull, 0x290031001f0016ull, 0x29002b801f0017ull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b00280000ull, 0x1002b00270001ull, 0x3002b00280003ull, 0x4002b00270004ull, 0x5002b00250005ull, 0x6002800300006ull, 0x7002700300007ull, 0x8002b00250008ull,
+    0x29002b00200015ull, 0x16002b80200016ull, 0x17002b80200017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000000ull, 0x15002b80210015ull, 0x16002b00210016ull, 0x17002b00210017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000000030003ull, 0x29000000060006ull, 0x15002b80220015ull, 0x16002b80220016ull, 0x17002200310017ull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x4000180030004ull, 0x5000280030005ull, 0x7000180060007ull, 0x8000280060008ull, 0x29002b0015000cull, 0x29002b0016000dull, 0x29002b0017000eull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000004ull, 0xd000c8003000dull, 0xe000c8006000eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000400070007ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000580070008ull, 0xe000d8007000eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000008ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x290008000e000eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xd000e8005000dull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x290004000d000dull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xc000d8001000cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xc000e8002000cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x290000000c000cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x9002b000c0018ull, 0xa002b000d0019ull, 0xb002b000e001aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29001a001b001full, 0x290019001c0020ull, 0x290018001d0021ull, 0x290019001e0022ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29001a00200020ull, 0x29001800220022ull, 0x290031001f0016ull, 0x29002b801f0017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29002b00200015ull, 0x16002b80200016ull, 0x17002b80200017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x15002b80210015ull, 0x16002b00210016ull, 0x17002b00210017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x15002b80220015ull, 0x16002b80220016ull, 0x17002200310017ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29002b0015000full, 0x29002b00160010ull, 0x29002b00170011ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xf000c002d000full, 0x10000d002d0010ull, 0x11000e002d0011ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x10000f80030010ull, 0x11000f80060011ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x11001080070011ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000800110011ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x10001180050010ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000400100010ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xf00108001000full, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xf00118002000full, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x290000000f000full, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29002b00150012ull, 0x29002b00160013ull, 0x29002b00170014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x12000c002e0012ull, 0x13000d002e0013ull, 0x14000e002e0014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x12000f002f0012ull, 0x130010002f0013ull, 0x140011002f0014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x13001280030013ull, 0x14001280060014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x14001380070014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000800140014ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x13001480050013ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000400130013ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x12001380010012ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x12001480020012ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x29000000120012ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
 };
-static __device__ const unsigned long long sv_fs[256] = {
-    0x1000000030001ull, 0x1000000060002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000100070002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000800000002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000200050001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000400000001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000100010000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000200020000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-};
-static __device__ const int diag[3] = {0, 4, 8};
 }  // namespace coop
 
 
@@ -325,124 +417,82 @@ struct Mech {
     return fmax(0.2, fmin(fac, 6.0));
   }
 
-  // ---- warp-cooperative attempt (tables + static warp schedules) ----
+  // ---- warp-cooperative attempt (static warp schedules) ----
   static constexpr int NPART = 6;
   static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
   static constexpr int D = NSLOTS + 4;     // partial derivatives
-  static constexpr int COOP_SLOTS = NSLOTS + 4 + NPART;
-  __device__ __forceinline__ static double acc_term(bool first, double acc, double coef, double t) {
-    if (first) return coef == 1.0 ? t : (coef == -1.0 ? -t : coef * t);
-    return coef == 1.0 ? acc + t : (coef == -1.0 ? acc - t : fma(coef, t, acc));
-  }
-
-  // F(y) into S[F..] for the state yv (S[Y..] or the stage state), cooperatively.
-  template <class KA>
-  __device__ __forceinline__ static void fun_coop(double* S, const double* yv, const KA& k, unsigned lane) {
-    namespace T = coop;
-    for (int r = lane; r < NR; r += 32) {
-      double q = k(r);
-      for (int e = T::r_off[r]; e < T::r_off[r + 1]; ++e) q = q * yv[T::r_y[e]];
-      S[Q + r] = q;
-    }
-    __syncwarp();
-    for (int i = lane; i < NV; i += 32) {
-      double v = 0.0;
-      for (int e = T::f_off[i]; e < T::f_off[i + 1]; ++e) v = acc_term(e == T::f_off[i], v, T::f_c[e], S[Q + T::f_r[e]]);
-      S[F + i] = v;
-    }
-    __syncwarp();
-  }
-
-  // Run a static warp schedule (emitter/warp_schedule.py) on S: one
-  // multiply-add, pivot multiply or reciprocal per lane and step, a warp
-  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by
-  // base.  The next two steps' words are in flight while one executes.
-  // Returns false if a reciprocal met a zero pivot.
-  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,
-                                                     int steps, int base, unsigned lane) {
+  static constexpr int CB = D + NPART;        // constants
+  static constexpr int NCONST = 9;
+  static constexpr int COOP_SLOTS = CB + NCONST;
+  // Run steps [s_begin, s_end) of the static warp schedule on S: one
+  // uniform operation S[out] = fma(+-S[a], S[b], S[c]) (or a pivot
+  // reciprocal) per lane and step, a warp barrier between steps.  The words
+  // of the next SCHED_AHEAD steps are in flight while the current ones
+  // execute; words past the end read as idle lanes.  Returns false if a
+  // reciprocal met a zero pivot.
+  static constexpr int SCHED_AHEAD = 8;
+  __device__ __forceinline__ static bool run_schedule(double* S, int s_begin, int s_end, unsigned lane) {
+    const unsigned long long* __restrict__ T = coop::sched;
     bool ok = true;
-    unsigned long long cur = __ldg(T + lane);
-    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;
-    for (int s = 0; s < steps; ++s) {
-      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;
-      const int kind = (int)(cur >> 48) & 3;
-      if (kind != 0) {
-        const int out = (int)(cur & 0xffffu) + base;
-        const int ia = (int)((cur >> 16) & 0xffffu);
-        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);
-        const double vo = S[out];
-        if (kind == 3) {
-          ok = ok && (vo != 0.0);
-          S[out] = 1.0 / vo;
-        } else {
-          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.
-          const double vb = S[ib];
-          const double x = kind == 1 ? -S[ia] : vo;
-          const double z = kind == 1 ? vo : -0.0;
-          S[out] = fma(x, vb, z);
-        }
+    unsigned long long cur[SCHED_AHEAD];
+    #pragma unroll
+    for (int j = 0; j < SCHED_AHEAD; ++j) {
+      const int s = s_begin + j;
+      cur[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;
+    }
+    for (int s0 = s_begin; s0 < s_end; s0 += SCHED_AHEAD) {
+      unsigned long long nxt[SCHED_AHEAD];
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) {
+        const int s = s0 + SCHED_AHEAD + j;
+        nxt[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;
       }
-      __syncwarp();
-      cur = nxt;
-      nxt = nn;
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) {
+        const unsigned long long w = cur[j];
+        const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+        const unsigned out = lo & 0xffffu;
+        if (out != 0xffffu) {
+          if (hi >> 31) {
+            const double v = S[out];
+            ok = ok && (v != 0.0);
+            S[out] = 1.0 / v;
+          } else {
+            // Negation flips the sign bit: exact, like -x in the per-thread code.
+            const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^
+                                                  ((long long)(lo >> 31) << 63));
+            S[out] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);
+          }
+        }
+        __syncwarp();
+      }
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) cur[j] = nxt[j];
     }
     return ok;
   }
 
-  // Solve (LU) x = b in place on S[base..].
-  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {
-    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);
-  }
-
   // One attempt by a whole warp on the cell held in shared memory S
-  // (NSLOTS + NR + NPART doubles).  Same values as attempt(); the error norm
-  // is summed by lane 0 in species order.  Returns err on every lane.
+  // (COOP_SLOTS doubles; the rate constants in the KT slots).  Same values
+  // as attempt(); the error norm is summed by lane 0 in species order.
+  // Returns err on every lane.
   template <class KA>
   __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,
                                                        unsigned lane) {
+    (void)k;
     namespace T = coop;
-    const double inv_g_dt = 1.0 / (GAMMA * h);
-    // Jacobian partials, then W into the LU slots.
-    for (int p = lane; p < NPART; p += 32) {
-      double d = k(T::d_r[p]);
-      for (int e = T::d_off[p]; e < T::d_off[p + 1]; ++e) {
-        const int f = T::d_fac[e];
-        d = d * (f < 0 ? T::d_lit[p] : S[Y + f]);
-      }
-      S[D + p] = d;
+    for (int i = lane; i < NCONST; i += 32) S[CB + i] = T::const_val[i];
+    __syncwarp();
+    if (lane == 0) {
+      S[CB + 3] = 1.0 / (GAMMA * h);
+      S[45] = -1.0156171083877703 / h;    // c21 / h
+      S[46] = 4.0759956452537702 / h;    // c31 / h
+      S[47] = 9.20767942983308 / h;    // c32 / h
     }
     __syncwarp();
-    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;
-    for (int w = lane; w < T::NW; w += 32) {
-      bool first = !T::w_diag[w];
-      double v = T::w_diag[w] ? inv_g_dt : 0.0;
-      for (int e = T::w_off[w]; e < T::w_off[w + 1]; ++e) {
-        v = acc_term(first, v, T::w_c[e], S[D + T::w_p[e]]);
-        first = false;
-      }
-      S[T::w_slot[w]] = v;
-    }
-    __syncwarp();
-    // LU by the static warp schedule (fill-in slots were zeroed with W).
-    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);
+    bool ok = true;
+    for (int st = 0; st < NSTAGE; ++st) ok = run_schedule(S, T::stage_step[st], T::stage_step[st + 1], lane) && ok;
     if (__any_sync(0xffffffffu, !ok)) status |= 1;
-    fun_coop(S, S + Y, k, lane);
-    for (int i = lane; i < NV; i += 32) S[12 + i] = S[F + i];
-    __syncwarp();
-    solve_coop(S, 12, lane);
-    // Stage state into the DY slots (free until the error block).
-    for (int i = lane; i < NV; i += 32) S[DY + i] = S[Y + i] + S[12 + i];
-    __syncwarp();
-    fun_coop(S, S + DY, k, lane);
-    const double c21 = -1.0156171083877703 / h;
-    for (int i = lane; i < NV; i += 32) S[15 + i] = fma(c21, S[12 + i], S[F + i]);
-    __syncwarp();
-    solve_coop(S, 15, lane);
-    const double c31 = 4.0759956452537702 / h;
-    const double c32 = 9.20767942983308 / h;
-    for (int i = lane; i < NV; i += 32) S[18 + i] = fma(c32, S[15 + i], fma(c31, S[12 + i], S[F + i]));
-    __syncwarp();
-    solve_coop(S, 18, lane);
     // Increment, and q_i^2 of the error norm into the rate slots.
     for (int i = lane; i < NV; i += 32) {
       const double k0 = S[12 + i];

@@ -7,158 +7,346 @@ namespace mkpp_small_strato {
 
 // Tables of the warp-cooperative attempt (device constant data).
 namespace coop {
-static __device__ const int r_off[11] = {0, 1, 3, 4, 6, 7, 8, 10, 12, 14, 15};
-static __device__ const int r_y[15] = {2, 1, 2, 3, 1, 3, 3, 0, 0, 3, 4, 3, 5, 1, 5};
-static __device__ const int f_off[7] = {0, 3, 10, 18, 24, 27, 30};
-static __device__ const int f_r[30] = {4, 5, 6, 0, 1, 2, 3, 5, 8, 9, 0, 1, 2, 3, 4, 6, 7, 8, 1, 2, 3, 4, 6, 7, 7, 8, 9, 7, 8, 9};
-static __device__ const double f_c[30] = {1.0, -1.0, -1.0, 2.0, -1.0, 1.0, -1.0, 1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 2.0, 1.0, 2.0, 1.0, 1.0, 1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, -1.0, -1.0};
-static __device__ const int d_r[15] = {0, 1, 1, 2, 3, 3, 4, 5, 6, 6, 7, 7, 8, 8, 9};
-static __device__ const int d_off[16] = {0, 0, 1, 2, 2, 3, 4, 4, 4, 5, 6, 7, 8, 9, 10, 10};
-static __device__ const int d_fac[10] = {2, 1, 3, 1, 3, 0, 3, 4, 1, 5};
-static __device__ const double d_lit[15] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
-static __device__ const int w_slot[26] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 19, 21, 22, 23, 24, 26, 27, 28};
-static __device__ const int w_diag[26] = {1, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-static __device__ const int w_off[27] = {0, 2, 4, 5, 8, 10, 12, 14, 15, 18, 20, 25, 26, 27, 28, 30, 31, 36, 37, 38, 39, 40, 42, 43, 44, 45, 47};
-static __device__ const int w_p[47] = {7, 8, 6, 9, 7, 1, 4, 13, 0, 2, 3, 5, 12, 14, 8, 1, 4, 13, 0, 2, 3, 5, 6, 9, 11, 10, 12, 8, 1, 4, 2, 3, 5, 6, 9, 11, 10, 13, 11, 10, 12, 14, 13, 11, 10, 12, 14};
-static __device__ const double w_c[47] = {1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, -2.0, 1.0, -1.0, 1.0, 1.0, -1.0, -2.0, 1.0, -2.0, -1.0, 1.0, 1.0, -1.0, -2.0, -1.0, -2.0, -1.0, -1.0, -1.0, 1.0, -1.0, 1.0, -1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, -1.0, 1.0, 1.0, -1.0, -1.0, 1.0, -1.0, -1.0, 1.0, 1.0};
-constexpr int NW = 26;
-constexpr int N_LU_ZERO = 3;
-static __device__ const int lu_zero[3] = {20, 25, 18};
-constexpr int LU_STEPS = 13;
-constexpr int SV_STEPS = 19;
-static __device__ const unsigned long long lu_fs[416] = {
-    0x3000000000000ull, 0x3000000000003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000000000002ull, 0x2000000000007ull, 0x200000000000dull, 0x2000300000008ull, 0x200030000000eull, 0x2000300000013ull, 0x2000300000018ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000100020005ull, 0x1000400080009ull, 0x100010007000aull, 0x100060008000cull, 0x10004000e000full, 0x1000400130014ull, 0x1000400180019ull, 0x10001000d0010ull,
-    0x10006000e0012ull, 0x1000600130017ull, 0x100060018001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x3000000000009ull, 0x100050008000aull, 0x10005000e0010ull, 0x1000500130015ull, 0x100050018001aull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x200090000000full, 0x2000900000014ull, 0x2000900000019ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000a000f0010ull, 0x1000b000f0011ull, 0x1000c000f0012ull, 0x1000a00140015ull, 0x1000a0019001aull, 0x1000b00140016ull, 0x1000c00140017ull, 0x1000b0019001bull,
-    0x1000c0019001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x3000000000010ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2001000000015ull, 0x200100000001aull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1001100150016ull, 0x1001200150017ull, 0x10011001a001bull, 0x10012001a001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x3000000000016ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x200160000001bull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10017001b001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x300000000001cull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
+static __device__ const double const_val[9] = {-0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, -2.0, 2.0};
+static __device__ const int stage_step[4] = {0, 31, 62, 84};
+static __device__ const unsigned long long sched[2688] = {
+    0x64006600410055ull, 0x64001f00420056ull, 0x64001e00420057ull, 0x64006600430058ull, 0x64002000440059ull, 0x64001e0044005aull, 0x6400660045005bull, 0x6400660046005cull,
+    0x6400200047005dull, 0x64001d0047005eull, 0x6400200048005full, 0x64002100480060ull, 0x64001e00490061ull, 0x64002200490062ull, 0x640066004a0063ull, 0x65006500650014ull,
+    0x65006500650019ull, 0x65006500650012ull, 0x64001f0041004bull, 0x64001e0042004cull, 0x6400200043004dull, 0x64001e0044004eull, 0x6400200045004full, 0x64001d00460050ull,
+    0x64001d00470051ull, 0x64002100480052ull, 0x64002200490053ull, 0x640022004a0054ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x670066005c0000ull, 0x640066805b0001ull, 0x640066805c0002ull, 0x67006600560003ull, 0x64006b00550004ull, 0x64006680580005ull, 0x64006600610006ull, 0x64006b005d0007ull,
+    0x64006600560008ull, 0x67006600550009ull, 0x6400668058000aull, 0x640066805f000bull, 0x640066005d000dull, 0x6400668056000eull, 0x6400668057000full, 0x67006600580010ull,
+    0x640066005f0011ull, 0x64006680620013ull, 0x64006600600015ull, 0x670066005f0016ull, 0x64006680610017ull, 0x64006600620018ull, 0x6400668060001aull, 0x6700660061001cull,
+    0x64001f004c004cull, 0x640020004e004eull, 0x64002000510051ull, 0x64002000520052ull, 0x64001e00530053ull, 0x640066004f0035ull, 0x64006c004b0036ull, 0x640066804b0037ull,
+    0x66005d0000ull, 0x10066005e0001ull, 0x3006600590003ull, 0x4006600570004ull, 0x50066005a0005ull, 0x6006680630006ull, 0x80059006b0008ull, 0x9006600570009ull,
+    0xa005a006b000aull, 0x6400668061000cull, 0xe00660059000eull, 0x100066005a0010ull, 0x17006680630017ull, 0x640066805f001bull, 0x1c00660063001cull, 0x35006680500035ull,
+    0x360066804c0036ull, 0x370066804c0037ull, 0x640066004c0038ull, 0x64006680520039ull, 0x6400660052003aull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x3006600620003ull, 0x8006680620008ull, 0xa0066805b000aull, 0x100066005b0010ull, 0x8000000000000000ull, 0x35006680510035ull, 0x360066004d0036ull, 0x370066004d0037ull,
+    0x380066804d0038ull, 0x39006600530039ull, 0x3a00668053003aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xa005e006b000aull, 0x100066005e0010ull, 0x64000000020002ull, 0x64000000070007ull, 0x640000000d000dull, 0x8000000000000003ull, 0x360066804e0036ull, 0x37004e006c0037ull,
+    0x380066804e0038ull, 0x39006600540039ull, 0x3a00668054003aull, 0x64006600350023ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xa00668060000aull, 0x10006600600010ull, 0x5000180020005ull, 0x64000300080008ull, 0x640003000e000eull, 0x64000300130013ull, 0x64000300180018ull, 0x36006600500036ull,
+    0x370066004f0037ull, 0x380066804f0038ull, 0x64006600390027ull, 0x640066003a0028ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x9000480080009ull, 0xa00018007000aull, 0xc00068008000cull, 0xf0004800e000full, 0x14000480130014ull, 0x19000480180019ull, 0x100001800d0010ull, 0x120006800e0012ull,
+    0x15000580130015ull, 0x1a00058018001aull, 0x17000680130017ull, 0x1c00068018001cull, 0x36006680530036ull, 0x370051006c0037ull, 0x38006680510038ull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000009ull, 0xa00058008000aull, 0x100005800e0010ull, 0x36006600540036ull, 0x37006600520037ull, 0x38006680520038ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640009000f000full, 0x64000900140014ull, 0x64000900190019ull, 0x37006600530037ull, 0x64006600360024ull, 0x64006600380026ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x10000a800f0010ull, 0x11000b800f0011ull, 0x12000c800f0012ull, 0x15000a80140015ull, 0x1a000a8019001aull, 0x16000b80140016ull, 0x17000c80140017ull, 0x1b000b8019001bull,
+    0x1c000c8019001cull, 0x64006600370025ull, 0x24002380020024ull, 0x260023800d0026ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000010ull, 0x25002380070025ull, 0x260024800e0026ull, 0x27002480130027ull, 0x28002480180028ull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001000150015ull, 0x640010001a001aull, 0x25002480080025ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x16001180150016ull, 0x17001280150017ull, 0x1b0011801a001bull, 0x1c0012801a001cull, 0x260025800f0026ull, 0x27002580140027ull, 0x28002580190028ull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x8000000000000016ull, 0x27002680150027ull, 0x280026801a0028ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640016001b001bull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x1c0017801b001cull, 0x280027801b0028ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x800000000000001cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001c00280028ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x27002880170027ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001600270027ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x26002780110026ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x26002880120026ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001000260026ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x250026800a0025ull, 0x23002680010023ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x250027800b0025ull, 0x64000000230023ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x250028800c0025ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64000900250025ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x24002580040024ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x24002680050024ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x24002880060024ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64000300240024ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x1d00660023003bull, 0x1e00660024003cull, 0x1f00660025003dull, 0x2000660026003eull, 0x2100660027003full, 0x22006600280040ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64003d0041004bull, 0x64003c0042004cull, 0x64003e0043004dull, 0x64003c0044004eull, 0x64003e0045004full, 0x64003b00460050ull, 0x64003b00470051ull, 0x64003f00480052ull,
+    0x64004000490053ull, 0x640040004a0054ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64003d004c004cull, 0x64003e004e004eull, 0x64003e00510051ull, 0x64003e00520052ull, 0x64003c00530053ull, 0x640066004f0035ull, 0x64006c004b0036ull, 0x640066804b0037ull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x35006680500035ull, 0x360066804c0036ull, 0x370066804c0037ull, 0x640066004c0038ull, 0x64006680520039ull, 0x6400660052003aull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x35006680510035ull, 0x360066004d0036ull, 0x370066004d0037ull, 0x380066804d0038ull, 0x39006600530039ull, 0x3a00668053003aull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x360066804e0036ull, 0x37004e006c0037ull, 0x380066804e0038ull, 0x39006600540039ull, 0x3a00668054003aull, 0x64006600350029ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x36006600500036ull, 0x370066004f0037ull, 0x380066804f0038ull, 0x29002300680029ull, 0x6400660039002dull, 0x640066003a002eull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x36006680530036ull, 0x370051006c0037ull, 0x38006680510038ull, 0x2d00270068002dull, 0x2e00280068002eull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x36006600540036ull, 0x37006600520037ull, 0x38006680520038ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x37006600530037ull, 0x6400660036002aull, 0x6400660038002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2a00240068002aull, 0x6400660037002bull, 0x2c00260068002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b00250068002bull, 0x2a00298002002aull, 0x2c0029800d002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b00298007002bull, 0x2c002a800e002cull, 0x2d002a8013002dull, 0x2e002a8018002eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b002a8008002bull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2c002b800f002cull, 0x2d002b8014002dull, 0x2e002b8019002eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2d002c8015002dull, 0x2e002c801a002eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2e002d801b002eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001c002e002eull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2d002e8017002dull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640016002d002dull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2c002d8011002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2c002e8012002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640010002c002cull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b002c800a002bull, 0x29002c80010029ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b002d800b002bull, 0x64000000290029ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2b002e800c002bull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640009002b002bull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2a002b8004002aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2a002c8005002aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2a002e8006002aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x640003002a002aull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x6400660035002full, 0x64006600360030ull, 0x64006600370031ull, 0x64006600380032ull, 0x64006600390033ull, 0x640066003a0034ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2f00230069002full, 0x30002400690030ull, 0x31002500690031ull, 0x32002600690032ull, 0x33002700690033ull, 0x34002800690034ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x2f0029006a002full, 0x30002a006a0030ull, 0x31002b006a0031ull, 0x32002c006a0032ull, 0x33002d006a0033ull, 0x34002e006a0034ull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x30002f80020030ull, 0x31002f80070031ull, 0x32002f800d0032ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x31003080080031ull, 0x320030800e0032ull, 0x33003080130033ull, 0x34003080180034ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x320031800f0032ull, 0x33003180140033ull, 0x34003180190034ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x33003280150033ull, 0x340032801a0034ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x340033801b0034ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001c00340034ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x33003480170033ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001600330033ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x32003380110032ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x32003480120032ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64001000320032ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x310032800a0031ull, 0x2f00328001002full, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x310033800b0031ull, 0x640000002f002full, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x310034800c0031ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64000900310031ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x30003180040030ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x30003280050030ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x30003480060030ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0x64000300300030ull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
+    0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
 };
-static __device__ const unsigned long long sv_fs[608] = {
-    0x1000000020001ull, 0x1000000070002ull, 0x10000000d0003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000100080002ull, 0x10001000e0003ull, 0x1000100130004ull, 0x1000100180005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10002000f0003ull, 0x1000200140004ull, 0x1000200190005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000300150004ull, 0x10003001a0005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10004001b0005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2001c00000005ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000500170004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2001600000004ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000400110003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000500120003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2001000000003ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10003000a0002ull, 0x1000300010000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10004000b0002ull, 0x2000000000000ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x10005000c0002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000900000002ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000200040001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000300050001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x1000500060001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x2000300000001ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-    0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull, 0x0ull,
-};
-static __device__ const int diag[6] = {0, 3, 9, 16, 22, 28};
 }  // namespace coop
 
 
@@ -546,124 +734,82 @@ struct Mech {
     return fmax(0.2, fmin(fac, 6.0));
   }
 
-  // ---- warp-cooperative attempt (tables + static warp schedules) ----
+  // ---- warp-cooperative attempt (static warp schedules) ----
   static constexpr int NPART = 15;
   static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
   static constexpr int D = NSLOTS + 10;     // partial derivatives
-  static constexpr int COOP_SLOTS = NSLOTS + 10 + NPART;
-  __device__ __forceinline__ static double acc_term(bool first, double acc, double coef, double t) {
-    if (first) return coef == 1.0 ? t : (coef == -1.0 ? -t : coef * t);
-    return coef == 1.0 ? acc + t : (coef == -1.0 ? acc - t : fma(coef, t, acc));
-  }
-
-  // F(y) into S[F..] for the state yv (S[Y..] or the stage state), cooperatively.
-  template <class KA>
-  __device__ __forceinline__ static void fun_coop(double* S, const double* yv, const KA& k, unsigned lane) {
-    namespace T = coop;
-    for (int r = lane; r < NR; r += 32) {
-      double q = k(r);
-      for (int e = T::r_off[r]; e < T::r_off[r + 1]; ++e) q = q * yv[T::r_y[e]];
-      S[Q + r] = q;
-    }
-    __syncwarp();
-    for (int i = lane; i < NV; i += 32) {
-      double v = 0.0;
-      for (int e = T::f_off[i]; e < T::f_off[i + 1]; ++e) v = acc_term(e == T::f_off[i], v, T::f_c[e], S[Q + T::f_r[e]]);
-      S[F + i] = v;
-    }
-    __syncwarp();
-  }
-
-  // Run a static warp schedule (emitter/warp_schedule.py) on S: one
-  // multiply-add, pivot multiply or reciprocal per lane and step, a warp
-  // barrier between steps.  `out`, and `b` of a multiply-add, are offset by
-  // base.  The next two steps' words are in flight while one executes.
-  // Returns false if a reciprocal met a zero pivot.
-  __device__ __forceinline__ static bool run_schedule(double* S, const unsigned long long* __restrict__ T,
-                                                     int steps, int base, unsigned lane) {
+  static constexpr int CB = D + NPART;        // constants
+  static constexpr int NCONST = 9;
+  static constexpr int COOP_SLOTS = CB + NCONST;
+  // Run steps [s_begin, s_end) of the static warp schedule on S: one
+  // uniform operation S[out] = fma(+-S[a], S[b], S[c]) (or a pivot
+  // reciprocal) per lane and step, a warp barrier between steps.  The words
+  // of the next SCHED_AHEAD steps are in flight while the current ones
+  // execute; words past the end read as idle lanes.  Returns false if a
+  // reciprocal met a zero pivot.
+  static constexpr int SCHED_AHEAD = 8;
+  __device__ __forceinline__ static bool run_schedule(double* S, int s_begin, int s_end, unsigned lane) {
+    const unsigned long long* __restrict__ T = coop::sched;
     bool ok = true;
-    unsigned long long cur = __ldg(T + lane);
-    unsigned long long nxt = steps > 1 ? __ldg(T + 32 + lane) : 0ull;
-    for (int s = 0; s < steps; ++s) {
-      const unsigned long long nn = s + 2 < steps ? __ldg(T + (size_t)(s + 2) * 32 + lane) : 0ull;
-      const int kind = (int)(cur >> 48) & 3;
-      if (kind != 0) {
-        const int out = (int)(cur & 0xffffu) + base;
-        const int ia = (int)((cur >> 16) & 0xffffu);
-        const int ib = (int)((cur >> 32) & 0xffffu) + (kind == 1 ? base : 0);
-        const double vo = S[out];
-        if (kind == 3) {
-          ok = ok && (vo != 0.0);
-          S[out] = 1.0 / vo;
-        } else {
-          // fma(-a, b, o) for a multiply-add; fma(o, b, -0.0) == o * b exactly.
-          const double vb = S[ib];
-          const double x = kind == 1 ? -S[ia] : vo;
-          const double z = kind == 1 ? vo : -0.0;
-          S[out] = fma(x, vb, z);
-        }
+    unsigned long long cur[SCHED_AHEAD];
+    #pragma unroll
+    for (int j = 0; j < SCHED_AHEAD; ++j) {
+      const int s = s_begin + j;
+      cur[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;
+    }
+    for (int s0 = s_begin; s0 < s_end; s0 += SCHED_AHEAD) {
+      unsigned long long nxt[SCHED_AHEAD];
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) {
+        const int s = s0 + SCHED_AHEAD + j;
+        nxt[j] = s < s_end ? __ldg(T + (size_t)s * 32 + lane) : 0xffffull;
       }
-      __syncwarp();
-      cur = nxt;
-      nxt = nn;
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) {
+        const unsigned long long w = cur[j];
+        const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+        const unsigned out = lo & 0xffffu;
+        if (out != 0xffffu) {
+          if (hi >> 31) {
+            const double v = S[out];
+            ok = ok && (v != 0.0);
+            S[out] = 1.0 / v;
+          } else {
+            // Negation flips the sign bit: exact, like -x in the per-thread code.
+            const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^
+                                                  ((long long)(lo >> 31) << 63));
+            S[out] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);
+          }
+        }
+        __syncwarp();
+      }
+      #pragma unroll
+      for (int j = 0; j < SCHED_AHEAD; ++j) cur[j] = nxt[j];
     }
     return ok;
   }
 
-  // Solve (LU) x = b in place on S[base..].
-  __device__ __forceinline__ static void solve_coop(double* S, int base, unsigned lane) {
-    run_schedule(S, coop::sv_fs, coop::SV_STEPS, base, lane);
-  }
-
   // One attempt by a whole warp on the cell held in shared memory S
-  // (NSLOTS + NR + NPART doubles).  Same values as attempt(); the error norm
-  // is summed by lane 0 in species order.  Returns err on every lane.
+  // (COOP_SLOTS doubles; the rate constants in the KT slots).  Same values
+  // as attempt(); the error norm is summed by lane 0 in species order.
+  // Returns err on every lane.
   template <class KA>
   __device__ __forceinline__ static double attempt_coop(double* S, const KA& k, double h, int& status,
                                                        unsigned lane) {
+    (void)k;
     namespace T = coop;
-    const double inv_g_dt = 1.0 / (GAMMA * h);
-    // Jacobian partials, then W into the LU slots.
-    for (int p = lane; p < NPART; p += 32) {
-      double d = k(T::d_r[p]);
-      for (int e = T::d_off[p]; e < T::d_off[p + 1]; ++e) {
-        const int f = T::d_fac[e];
-        d = d * (f < 0 ? T::d_lit[p] : S[Y + f]);
-      }
-      S[D + p] = d;
+    for (int i = lane; i < NCONST; i += 32) S[CB + i] = T::const_val[i];
+    __syncwarp();
+    if (lane == 0) {
+      S[CB + 3] = 1.0 / (GAMMA * h);
+      S[104] = -1.0156171083877703 / h;    // c21 / h
+      S[105] = 4.0759956452537702 / h;    // c31 / h
+      S[106] = 9.20767942983308 / h;    // c32 / h
     }
     __syncwarp();
-    for (int z = lane; z < T::N_LU_ZERO; z += 32) S[T::lu_zero[z]] = 0.0;
-    for (int w = lane; w < T::NW; w += 32) {
-      bool first = !T::w_diag[w];
-      double v = T::w_diag[w] ? inv_g_dt : 0.0;
-      for (int e = T::w_off[w]; e < T::w_off[w + 1]; ++e) {
-        v = acc_term(first, v, T::w_c[e], S[D + T::w_p[e]]);
-        first = false;
-      }
-      S[T::w_slot[w]] = v;
-    }
-    __syncwarp();
-    // LU by the static warp schedule (fill-in slots were zeroed with W).
-    const bool ok = run_schedule(S, T::lu_fs, T::LU_STEPS, 0, lane);
+    bool ok = true;
+    for (int st = 0; st < NSTAGE; ++st) ok = run_schedule(S, T::stage_step[st], T::stage_step[st + 1], lane) && ok;
     if (__any_sync(0xffffffffu, !ok)) status |= 1;
-    fun_coop(S, S + Y, k, lane);
-    for (int i = lane; i < NV; i += 32) S[35 + i] = S[F + i];
-    __syncwarp();
-    solve_coop(S, 35, lane);
-    // Stage state into the DY slots (free until the error block).
-    for (int i = lane; i < NV; i += 32) S[DY + i] = S[Y + i] + S[35 + i];
-    __syncwarp();
-    fun_coop(S, S + DY, k, lane);
-    const double c21 = -1.0156171083877703 / h;
-    for (int i = lane; i < NV; i += 32) S[41 + i] = fma(c21, S[35 + i], S[F + i]);
-    __syncwarp();
-    solve_coop(S, 41, lane);
-    const double c31 = 4.0759956452537702 / h;
-    const double c32 = 9.20767942983308 / h;
-    for (int i = lane; i < NV; i += 32) S[47 + i] = fma(c32, S[41 + i], fma(c31, S[35 + i], S[F + i]));
-    __syncwarp();
-    solve_coop(S, 47, lane);
     // Increment, and q_i^2 of the error norm into the rate slots.
     for (int i = lane; i < NV; i += 32) {
       const double k0 = S[35 + i];
