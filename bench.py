@@ -122,32 +122,26 @@ class ClockSampler:
 
 
 def dist_setup(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
+    """One process per GPU (torchrun); NCCL for our arm, gloo for the CPU
+    reference arm.  Cells shard with no data-path collective
+    (mkpp_gb300/shard.py)."""
+    from mkpp_gb300 import shard
 
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    return world, rank, local
+    env = shard.rank_env()
+    shard.init(env, "nccl" if args.impl == "ours" else "gloo")
+    return env.world, env.rank, env.local
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
+    from mkpp_gb300 import shard
 
-        dist.barrier()
+    shard.barrier()
 
 
 def max_over_ranks(x: float, world: int) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
+    from mkpp_gb300 import shard
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return shard.max_over_ranks(x)
 
 
 # ---------------------------------------------------------------------------
@@ -232,7 +226,9 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = workloads.make(args.workload, args.cells, seed=workloads.SEED + rank)
+    from mkpp_gb300 import shard
+
+    w = workloads.make(args.workload, args.cells, seed=shard.shard_seed(workloads.SEED, rank))
     hs = args.host_steps or w.host_steps
     n = w.ncells
     raw = load_raw(w.mechanism)
@@ -316,7 +312,7 @@ def main():
     el_ms = max_over_ranks(start.elapsed_time(end), world) / args.steps
     log(f"timed: {el_ms:.0f} ms per window")
     clk = clocks.summary()
-    cell_solves = n * hs * world
+    cell_solves = shard.sum_over_ranks(n * hs)
     value = cell_solves / (el_ms * 1e-3)
 
     # Work counters of the (deterministic) window just timed.
