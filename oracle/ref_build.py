@@ -109,6 +109,32 @@ def compile_driver(mech: str) -> Path:
     return out
 
 
+def shipped_lib_path(mech: str) -> Path:
+    return REF / f"libmkpp_ref_{mech}_shipped.so"
+
+
+def compile_shipped(mech: str, reference: str = DEFAULT_REFERENCE) -> Path | None:
+    """The driver against the reference's shipped generated solver
+    (``mkpp-generated/<mech>.hpp``, compiled where it lies, with its own
+    tolerances: the build behind the reference's native Kokkos reports).
+    None where the reference tree is absent."""
+    gen = Path(reference) / "mkpp-generated"
+    if not (gen / f"{mech}.hpp").exists():
+        return None
+    out = shipped_lib_path(mech)
+    src = HERE / "ref_driver.cpp"
+    if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+        return out
+    REF.mkdir(parents=True, exist_ok=True)
+    tmp = out.with_suffix(f".so.tmp{os.getpid()}")
+    cmd = [os.environ.get("CXX", "g++"), "-O3", "-std=c++20", "-fopenmp", "-shared", "-fPIC",
+           f"-I{HERE / 'kokkos_shim'}", f"-I{gen}", f"-DMKPP_REF_HEADER=\"{mech}.hpp\"",
+           f"-DMKPP_REF_NS=mkpp::generated::{mech}", str(src), "-o", str(tmp)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, out)
+    return out
+
+
 def build_if_available(reference: str = DEFAULT_REFERENCE) -> list[Path]:
     built = []
     for mech in MECHS:
@@ -122,11 +148,11 @@ def build_if_available(reference: str = DEFAULT_REFERENCE) -> list[Path]:
 class RefSolver:
     """The reference's generated integrate() on host cores, Oracle-like API."""
 
-    def __init__(self, mech: str):
+    def __init__(self, mech: str, path: Path | None = None):
         from mkpp_gb300.emitter.plan import load_raw
 
         self.raw = load_raw(mech)
-        self.lib = C.CDLL(str(lib_path(mech)))
+        self.lib = C.CDLL(str(path or lib_path(mech)))
         self.lib.mkpp_ref_integrate.restype = C.c_int
         self.lib.mkpp_ref_num_species.restype = C.c_int
         self.lib.mkpp_ref_num_parameters.restype = C.c_int

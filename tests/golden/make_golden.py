@@ -12,7 +12,18 @@ small JSON fixtures, so the tests never need the reference at run time:
   solve_plan tables of the shipped generated code
   (mkpp-generated/<mech>/supernodal_{factorize,solve}.hpp);
 * chapman_factorization_kat.json  the 13-slot known-answer test of
-  tests/integration/supernodal_factorization/test_factorization_parity.cpp.
+  tests/integration/supernodal_factorization/test_factorization_parity.cpp;
+* ts1_kokkos_2x300.json  final state of the reference's native Kokkos TS1 run
+  (reports/native-kokkos-5.1.1/final-mkpp-ts1.stdout.json) and its inputs:
+  initial state and 547 rate parameters
+  (benchmarks/solver_comparison/runners/mkpp/ts1_binding_data.hpp), the
+  two 300 s segments with photolysis slots scaled by 1.0 and 1.05, T and air
+  density (runners/mkpp/main.cpp:212-215, 333-344), and the tolerances of
+  the shipped generated solver (mkpp-generated/ts1.hpp);
+* ts1_reference_rates.json  F and the nonzero dense Jacobian entries of the
+  reference's own generated TS1 solver (compute_rates / compute_jacobian,
+  regenerated and compiled by oracle/ref_build.py) at the inputs above,
+  with the photolysis slots scaled by 1.0 and by 1.05.
 
 Usage: python tests/golden/make_golden.py --reference <MKPP checkout>
 """
@@ -73,6 +84,50 @@ def main():
     (HERE / "chapman_factorization_kat.json").write_text(json.dumps({
         "source": "tests/integration/supernodal_factorization/test_factorization_parity.cpp",
         "w": w, "rhs": [1.0, 2.0, 3.0, 4.0], "dense_logical": dense, "residual_tol": 1e-12}, indent=1))
+    binding = (ref / "benchmarks/solver_comparison/runners/mkpp/ts1_binding_data.hpp").read_text()
+
+    def arr(name, conv):
+        body = re.search(name + r"\{(.*?)\};", binding, re.S).group(1)
+        return [conv(x.strip()) for x in body.split(",") if x.strip()]
+
+    shipped = (ref / "mkpp-generated/ts1.hpp").read_text()
+    tol = {k: float(re.search(k + r"\[NUM_SPECIES\] = \{ *([^,]+),", shipped).group(1)) for k in ("atol", "rtol")}
+    run = json.loads((ref / "reports/native-kokkos-5.1.1/final-mkpp-ts1.stdout.json").read_text())
+    last = run["state"]["checkpoints"][-1]
+    (HERE / "ts1_kokkos_2x300.json").write_text(json.dumps({
+        "source": "reports/native-kokkos-5.1.1/final-mkpp-ts1.stdout.json",
+        "inputs": "benchmarks/solver_comparison/runners/mkpp/ts1_binding_data.hpp, main.cpp:212-215,333-344",
+        "tolerances": tol, "temperature": 287.45, "air_density": 42.393400541636808, "rh": 0.5,
+        "segments_s": [300.0, 300.0], "photolysis_slots": 123, "photolysis_scale": [1.0, 1.05],
+        "species": arr("species_names", lambda x: x.strip('"')),
+        "initial": arr("initial_state", float), "parameters": arr("reaction_parameters", float),
+        "final_time_s": last["time_seconds"], "final": last["values"],
+    }, separators=(",", ":")))
+    import sys
+
+    import numpy as np
+
+    sys.path.insert(0, str(HERE.parent.parent))
+    from oracle import ref_build
+
+    ref_build.generate("ts1", str(ref))
+    ref_build.compile_driver("ts1")
+    solver = ref_build.RefSolver("ts1")
+    binding_inputs = json.loads((HERE / "ts1_kokkos_2x300.json").read_text())
+    cases = []
+    for scale in binding_inputs["photolysis_scale"]:
+        P = np.array(binding_inputs["parameters"])[:, None].copy()
+        P[:binding_inputs["photolysis_slots"]] *= scale
+        conc = np.array(binding_inputs["initial"])[:, None]
+        F, J = solver.evaluate(conc, np.array([binding_inputs["temperature"]]),
+                               np.array([binding_inputs["air_density"]]), np.array([binding_inputs["rh"]]), P)
+        nz = np.argwhere(J[:, :, 0] != 0.0)
+        cases.append({"photolysis_scale": scale, "F": F[:, 0].tolist(),
+                      "J": [[int(i), int(j), float(J[i, j, 0])] for i, j in nz]})
+    (HERE / "ts1_reference_rates.json").write_text(json.dumps({
+        "source": "reference compute_rates / compute_jacobian (mkpp-generated/ts1.hpp, regenerated)",
+        "inputs": "ts1_kokkos_2x300.json (initial state, parameters, temperature, air density, rh)",
+        "cases": cases}, separators=(",", ":")))
     print("fixtures written to", HERE)
 
 

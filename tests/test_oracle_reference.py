@@ -94,3 +94,69 @@ def test_integrate_matches_reference_saprc99_statistically():
     # A cell the reference leaves non-finite is one the port flags.
     bad_ref = ~np.isfinite(rr["conc"]).all(axis=0)
     assert np.all(ro["status"][bad_ref] != 0)
+
+
+# ---------------------------------------------------------------------------
+# TS1 (210 species, 547 reactions, 547 runtime parameters).  Pinned at the
+# tendency and Jacobian level against fixtures of the reference's own
+# generated solver (tests/golden/ts1_reference_rates.json, made by
+# tests/golden/make_golden.py through oracle/ref_build.py), at the inputs of
+# the reference's native TS1 run.  The final state of that run
+# (reports/native-kokkos-5.1.1/final-mkpp-ts1.stdout.json) is not a usable
+# pin for integrate(): the shipped TS1 header, compiled here behind the same
+# driver at its own tolerances, goes non-finite on that schedule, and its
+# report states the run came from a separate generation and "checks
+# execution, not calibrated scientific equivalence".  Like SAPRC99, TS1 has
+# tendencies of order 1e30 from its Troe rates, so the trajectory depends on
+# rounding details.
+
+def _ts1_golden():
+    import json
+    from pathlib import Path
+
+    here = Path(__file__).resolve().parent / "golden"
+    return (json.loads((here / "ts1_kokkos_2x300.json").read_text()),
+            json.loads((here / "ts1_reference_rates.json").read_text()))
+
+
+def test_ts1_tendencies_and_jacobian_match_reference_fixture():
+    g, rates = _ts1_golden()
+    o = Oracle("ts1")
+    assert o.raw["species"] == g["species"]
+    conc = np.array(g["initial"])[:, None]
+    env = (np.array([g["temperature"]]), np.array([g["air_density"]]), np.array([g["rh"]]))
+    for case in rates["cases"]:
+        P = np.array(g["parameters"])[:, None].copy()
+        P[:g["photolysis_slots"]] *= case["photolysis_scale"]
+        F1, Jc = o.evaluate(conc, *env, param=P)
+        F0 = np.array(case["F"])
+        assert np.abs(F1[:, 0] - F0).max() <= 1e-13 * np.abs(F0).max()
+        J1 = o.dense_jacobian(Jc)[:, :, 0]
+        J0 = np.zeros_like(J1)
+        for i, j, v in case["J"]:
+            J0[i, j] = v
+        nz = J0 != 0
+        assert not np.any(J1[~nz])
+        assert (np.abs(J1 - J0)[nz] / np.abs(J0[nz])).max() < 1e-11
+
+
+def test_ts1_oracle_runs_the_native_schedule():
+    """Smoke: the 2 x 300 s schedule of the native run, at the shipped
+    solver's tolerances, ends with status 0 and finite values."""
+    from mkpp_gb300.emitter.plan import load_raw
+
+    g, _ = _ts1_golden()
+    raw = load_raw("ts1")
+    ns = len(raw["species"])
+    raw["atol"] = [g["tolerances"]["atol"]] * ns
+    raw["rtol"] = [g["tolerances"]["rtol"]] * ns
+    o = Oracle(raw)
+    conc = np.array(g["initial"])[:, None].copy()
+    env = dict(temp=np.array([g["temperature"]]), rho=np.array([g["air_density"]]), rh=np.array([g["rh"]]))
+    for dt, scale in zip(g["segments_s"], g["photolysis_scale"]):
+        P = np.array(g["parameters"])[:, None].copy()
+        P[:g["photolysis_slots"]] *= scale
+        r = o.integrate(conc, dt, 1, param=P, **env)
+        conc = r["conc"]
+        assert np.all(r["status"] == 0)
+    assert np.isfinite(conc).all()
