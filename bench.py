@@ -361,6 +361,9 @@ def main():
             "peak_source": "measured live: DFMA probe (csrc/probe.cu) on this GPU",
             "kernel": "integrate_persistent_kernel", "launch_ms_avg": kernel_avg_ms,
             "algorithmic_flops_per_launch": flops_run,
+            # No DRAM capture of this build at this size; the last ncu capture
+            # (an earlier build, capped case) read+wrote 97 KB per attempt,
+            # about a quarter of HBM bandwidth at the FP64-bound attempt rate.
             "traffic": None,
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
         },

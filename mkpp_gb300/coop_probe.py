@@ -1,4 +1,4 @@
-"""Latency of the warp-cooperative attempt against one lane per cell.
+"""Attempt latency and throughput of the integrate kernels.
 
     python -m mkpp_gb300.coop_probe CELLS ATTEMPTS DEFER [MECHANISM]
 
@@ -7,7 +7,10 @@ rate constants from the workload) with a bound of ATTEMPTS attempts per cell
 through the persistent kernel, parking every cell after DEFER attempts
 (0: never).  With DEFER = 1 each cell makes one attempt on a lane and the rest
 on a whole warp; with DEFER = 0 all of them on its lane.  Few cells (one per
-SM or fewer) make the time the latency of one cell's attempts.  Prints the
+SM or fewer) make the time the latency of one cell's attempts; many cells
+with DEFER = 0 and a small ATTEMPTS bound give the persistent kernel's
+throughput with every lane busy (no tail), a case small enough for ncu.
+Prints the
 wall time of each of two repetitions (CUDA synchronised on both sides), the
 attempts made and the rate.  Used to choose `mkpp_set_launch_tuning`'s
 defer_after.
