@@ -10,10 +10,9 @@ on a whole warp; with DEFER = 0 all of them on its lane.  Few cells (one per
 SM or fewer) make the time the latency of one cell's attempts; many cells
 with DEFER = 0 and a small ATTEMPTS bound give the persistent kernel's
 throughput with every lane busy (no tail), a case small enough for ncu.
-Prints the
-wall time of each of two repetitions (CUDA synchronised on both sides), the
-attempts made and the rate.  Used to choose `mkpp_set_launch_tuning`'s
-defer_after.
+Prints the wall time of each of two repetitions (CUDA synchronised on both
+sides), the attempts made and the rate.  Used to choose
+`mkpp_set_launch_tuning`'s defer_after.
 """
 
 from __future__ import annotations
