@@ -121,6 +121,7 @@ struct LaunchConfig {
   int sms = 0;
   int coop_warps = 0;
   size_t coop_smem = 0;
+  bool coop_ok = false;
 };
 
 template <int MINB>
@@ -144,11 +145,13 @@ const LaunchConfig& launch_config() {
     int per_sm = cfg.minb == 4 ? resident_blocks4() : resident_blocks<2>();
     if (t.blocks_per_sm > 0) per_sm = std::min(per_sm, t.blocks_per_sm);
     cfg.grid = cfg.sms * per_sm;
-    // Cooperative kernel: as many warps per block as fit in 200 KB of shared memory.
+    // Cooperative kernel: as many warps per block (at most kCoopWarps) as fit
+    // in 200 KB of shared memory.  A cell store larger than that leaves the
+    // cooperative kernel unused (no parking).
     const size_t per_warp = (size_t)Mech::COOP_SLOTS * sizeof(double);
-    cfg.coop_warps = (int)std::max<size_t>(1, std::min<size_t>(4, (200u * 1024u) / per_warp));
-    cfg.coop_smem = per_warp * cfg.coop_warps;
-    set_coop_smem(cfg.coop_smem);
+    cfg.coop_warps = (int)std::min<size_t>(mkpp::kCoopWarps, (200u * 1024u) / per_warp);
+    cfg.coop_smem = per_warp * (size_t)std::max(1, cfg.coop_warps);
+    cfg.coop_ok = cfg.coop_warps >= 1 && set_coop_smem(cfg.coop_smem) == MKPP_SUCCESS;
   }
   return cfg;
 }
@@ -192,7 +195,7 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   if (mode == 1) {
     const long long park = (long long)tuning().defer_after * std::max(1, a.steps);
     a.defer_after = (int)std::min<long long>(park, INT32_MAX);
-    a.defer = a.defer_after > 0 ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
+    a.defer = a.defer_after > 0 && cfg.coop_ok ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
     if (!a.defer) a.defer_after = 0;
     if (cfg.minb == 4) {
       if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;

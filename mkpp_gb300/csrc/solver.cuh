@@ -415,10 +415,11 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
   extern __shared__ double smem[];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned wib = threadIdx.x >> 5;
+  const unsigned wpb = blockDim.x >> 5;  // warps launched per block (<= kCoopWarps)
   double* S = smem + (size_t)wib * Mech::COOP_SLOTS;
   const size_t n = (size_t)a.ncells;
   const unsigned count = *a.defer_count;
-  for (unsigned idx = blockIdx.x * kCoopWarps + wib; idx < count; idx += gridDim.x * kCoopWarps) {
+  for (unsigned idx = blockIdx.x * wpb + wib; idx < count; idx += gridDim.x * wpb) {
     const Deferred d = a.defer[idx];
     const size_t c = (size_t)d.cell;
     for (int i = lane; i < Mech::NV; i += 32) S[Mech::Y + i] = a.conc[c + n * Mech::var_phys(i)];

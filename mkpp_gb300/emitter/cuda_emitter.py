@@ -60,15 +60,6 @@ class _Code:
         return "\n".join(self.lines) + "\n"
 
 
-def _monomial(terms: list[tuple[int, int]], yname: str, v2l: dict[int, int]) -> list[str]:
-    """Factors of prod y^nu for (physical species, power) pairs, logical indices."""
-    fac = []
-    for s, pw in terms:
-        for _ in range(pw):
-            fac.append(f"{yname}[{v2l[s]}]")
-    return fac
-
-
 def _accumulate(target: str, init: str | None, terms: list[tuple[float, str]]) -> str:
     """Sum ``init + c1*t1 + c2*t2 ...`` left to right, exact signs for +-1."""
     expr = init
@@ -128,15 +119,6 @@ def _interleave(c, plan, ops, operands, scale):
                 c(f"      S[{out}] = v{out};")
 
 
-def _levels(deps_of, n):
-    """Longest-path level of items 0..n-1 given deps_of(i) (earlier items)."""
-    lev = [0] * n
-    for i in range(n):
-        d = deps_of(i)
-        lev[i] = 1 + max((lev[j] for j in d), default=-1)
-    return lev
-
-
 def _c_array(c, ctype, name, values):
     vals = list(values) or [0]
     body = ", ".join(str(v) for v in vals)
@@ -152,7 +134,7 @@ def _c_u64_array(c, name, values):
     c("};")
 
 
-def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None):
+def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots):
     """Warp-cooperative form of one attempt: the same arithmetic, operation by
     operation, as ``attempt``, with each tableau stage run as a static 32-lane
     schedule (``warp_schedule``).  Used for the few cells whose step count
@@ -970,7 +952,7 @@ def emit_mechanism(plan: ReducedPlan) -> str:
         c(f"    const double fac = 0.9 * pow(err, -{_lit(1.0 / elo)});")
     c("    return fmax(0.2, fmin(fac, 6.0));")
     c("  }")
-    _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots, mterms_all=None)
+    _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots)
     _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots)
     c("};")
     c("")
