@@ -39,6 +39,7 @@ struct DeviceBuffers {
   int* accepted = nullptr;
   int* rejected = nullptr;
   void* workspace = nullptr;
+  size_t workspace_bytes = 0;  // grows when a launch-tuning change enlarges the grid
 };
 
 }  // namespace
@@ -453,8 +454,17 @@ static int ensure_device(mkpp_handle_s* h, size_t out_bytes) {
     MKPP_CUDA(h, cudaMalloc(&d.status, n * sizeof(int)));
     MKPP_CUDA(h, cudaMalloc(&d.accepted, n * sizeof(int)));
     MKPP_CUDA(h, cudaMalloc(&d.rejected, n * sizeof(int)));
-    MKPP_CUDA(h, cudaMalloc(&d.workspace, workspace_bytes(n)));
     d.cells = n;
+  }
+  // The integrate scratch depends on the launch grid, which
+  // mkpp_set_launch_tuning can change between calls.
+  const size_t ws = workspace_bytes(n);
+  if (ws > d.workspace_bytes) {
+    cudaFree(d.workspace);
+    d.workspace = nullptr;
+    d.workspace_bytes = 0;
+    MKPP_CUDA(h, cudaMalloc(&d.workspace, ws));
+    d.workspace_bytes = ws;
   }
   if (out_bytes > d.out_bytes) {
     cudaFree(d.out);
