@@ -1,0 +1,146 @@
+"""The emitted GPU arithmetic, run on the host (CPU).
+
+The per-thread attempt of each generated header (mkpp_gb300/generated/<m>.cuh)
+is compiled for the host through tests/hostsim/.  The CUDA qualifiers become
+plain C++, and -ffp-contract=off lets only explicit fma() calls fuse, as in
+the GPU build (--fmad=false).  For one attempt on seeded cells:
+* the two emitted forms agree bit for bit: the per-thread attempt's stage
+  vectors and factorised LU slots equal those of the cooperative kernel's
+  stage programs, executed in program order with exactly rounded fma;
+* the accepted step agrees with the oracle's step with the same step size
+  forced, per species to 1e-9 (|oracle| + atol), the GPU parity gate.  The
+  two formulations differ at round-off, and a single step amplifies that by
+  cond(W): measured, the difference tracks eps * cond(W) (Chapman 5e-16,
+  small_strato 1e-12 at cond 1e5, SAPRC99 2.5e-10 at cond 3e8).  So the
+  step size per mechanism keeps cond(W) below ~1e9 on these cells.
+SAPRC99 runs with its three 1e33-1e37 1/s rate constants moderated to 1e3,
+as in the GPU forced-step test.
+"""
+
+import ctypes as C
+import subprocess
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mkpp_gb300 import workloads
+from mkpp_gb300.emitter import cuda_emitter
+from mkpp_gb300.emitter import warp_schedule as ws
+from mkpp_gb300.emitter.plan import load
+from oracle.oracle import Oracle
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+MECHS = ["chapman", "small_strato", "saprc99"]
+# Step sizes of the oracle comparison: cond(W) at most ~10, 1.5e5 and 3e8.
+H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6}
+EXTREME = {"saprc99": (11, 32, 69)}
+
+
+@pytest.fixture(scope="module")
+def hostsim(tmp_path_factory):
+    out = tmp_path_factory.mktemp("hostsim")
+    libs = {}
+    for m in MECHS:
+        so = out / f"hostsim_{m}.so"
+        subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
+                        f"-I{HERE / 'hostsim'}", f"-I{ROOT / 'mkpp_gb300' / 'generated'}",
+                        f"-I{ROOT / 'mkpp_gb300' / 'csrc'}", f'-DMKPP_MECH_HEADER="{m}.cuh"',
+                        f"-DMKPP_MECH_NS=mkpp_{m}", str(HERE / "hostsim" / "attempt_driver.cpp"), "-o", str(so)],
+                       check=True)
+        lib = C.CDLL(str(so))
+        lib.hostsim_attempt.restype = C.c_double
+        lib.hostsim_attempt.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+        libs[m] = lib
+    return libs
+
+
+def _layout(lib):
+    v = (C.c_int * 9)()
+    lib.hostsim_layout(v)
+    return dict(zip(("NSLOTS", "NV", "NR", "NSTAGE", "Y", "K0", "F", "DY", "KT"), list(v)))
+
+
+def _xfma(a, b, c):
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def _run_programs(progs, S):
+    S = list(S)
+    for ops in progs:
+        for kind, out, a, b, c, neg in ops:
+            if kind == ws.RCP:
+                S[out] = 1.0 / S[out]
+            else:
+                S[out] = _xfma(-S[a] if neg else S[a], S[b], S[c])
+    return np.array(S)
+
+
+def _case(mech, n=4):
+    w = workloads.make(mech, n)
+    o = Oracle(mech)
+    k, dk = o.rate_constants(w.conc, w.temp, w.rho, w.rh, None, w.param)
+    for r in EXTREME.get(mech, ()):
+        k[r] = np.minimum(k[r], 1e3)
+    return w, o, k, dk
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_per_thread_attempt_equals_cooperative_programs(hostsim, mech):
+    lib = hostsim[mech]
+    L = _layout(lib)
+    plan = load(mech)
+    cuda_emitter.emit_mechanism(plan)
+    progs, _, info = plan._coop_programs
+    assert (info["Y"], info["K0"], info["FS"], info["DY"], info["KT"]) == (L["Y"], L["K0"], L["F"], L["DY"], L["KT"])
+    w, o, k, _ = _case(mech)
+    nv, nlu = L["NV"], len(plan.lu_slots)
+    h = 10.0
+    for c in range(w.ncells):
+        y = np.ascontiguousarray(w.conc[plan.var_phys, c])
+        kc = np.ascontiguousarray(k[:, c])
+        S = np.zeros(L["NSLOTS"])
+        S[L["Y"]:L["Y"] + nv] = y
+        st = C.c_int(0)
+        lib.hostsim_attempt(S.ctypes.data, kc.ctypes.data, h, C.byref(st))
+        P = np.zeros(info["slots"])
+        P[info["Y"]:info["Y"] + nv] = y
+        P[info["KT"]:info["KT"] + len(kc)] = kc
+        CB = info["CB"]
+        P[CB:CB + 4] = (-0.0, 0.0, 1.0, 1.0 / (plan.tableau["Gamma"][0] * h))
+        for (s_, j), slot in info["cterm_slot"].items():
+            P[slot] = info["C"][(s_ - 1) * (s_ - 2) // 2 + j - 1] / h
+        for v, slot in info["literals"].items():
+            P[slot] = v
+        P = _run_programs(progs, P)
+        K = slice(L["K0"], L["K0"] + L["NSTAGE"] * nv)
+        assert st.value == 0
+        assert np.array_equal(S[K], P[K])
+        assert np.array_equal(S[:nlu], P[:nlu])
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_per_thread_step_matches_oracle_with_forced_step(hostsim, mech):
+    lib = hostsim[mech]
+    L = _layout(lib)
+    plan = load(mech)
+    w, o, k, dk = _case(mech, 8)
+    nv = L["NV"]
+    h = H_ORACLE[mech]
+    for c in range(w.ncells):
+        y = np.ascontiguousarray(w.conc[plan.var_phys, c])
+        kc = np.ascontiguousarray(k[:, c])
+        S = np.zeros(L["NSLOTS"])
+        S[L["Y"]:L["Y"] + nv] = y
+        st = C.c_int(0)
+        lib.hostsim_attempt(S.ctypes.data, kc.ctypes.data, h, C.byref(st))
+        assert st.value == 0
+        ynew = y + S[L["DY"]:L["DY"] + nv]
+        rep = o.integrate(w.conc[:, c:c + 1].copy(), h, k=k[:, c:c + 1].copy(), dk=dk[:, c:c + 1].copy(),
+                          temp=w.temp[c:c + 1], rho=w.rho[c:c + 1], rh=w.rh[c:c + 1], param=w.param[:, c:c + 1],
+                          replay=(np.array([[h]]), np.array([[1]], np.uint8), np.array([1], np.int32)))
+        ref = rep["conc"][plan.var_phys, 0]
+        atol = np.array(o.raw["atol"])[plan.var_phys]
+        assert np.all(np.abs(ynew - ref) <= 1e-9 * (np.abs(ref) + atol))
