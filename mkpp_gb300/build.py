@@ -23,7 +23,7 @@ LIB = PKG / "lib"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99")
+DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99", "ts1")
 
 
 def nvcc() -> str:
@@ -44,9 +44,27 @@ UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_capi.c
          "mkpp_persist4.cu", "mkpp_eval.cu", "mkpp_coop.cu", "mkpp_diff.cu")
 
 
+# Units of a table-driven mechanism (too large to unroll, such as TS1): its
+# header has no adjoint, and the unrolled F/J evaluation kernels would take
+# minutes to compile, so the differentiation and evaluation entries are stubs.
+DIFF_UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_diff.cu", "mkpp_eval.cu")
+
+
+def is_table(mech: str) -> bool:
+    """True if the mechanism's generated header walks tables instead of
+    unrolled code (read from the header, which the emitter writes first)."""
+    return "TABLE_ATTEMPT = true" in (GEN / f"{mech}.cuh").read_text()
+
+
+def units(mech: str) -> tuple[str, ...]:
+    if is_table(mech):
+        return tuple(u for u in UNITS if u not in DIFF_UNITS) + ("mkpp_diff_stub.cu", "mkpp_eval_stub.cu")
+    return UNITS
+
+
 def _sources(mech: str) -> list[Path]:
-    return [*(CSRC / u for u in UNITS), CSRC / "capi_common.cuh", CSRC / "solver.cuh", CSRC / "mkpp_device.cuh",
-            GEN / f"{mech}.cuh", INCLUDE / "mkpp.h", Path(__file__)]
+    return [*(CSRC / u for u in units(mech)), CSRC / "capi_common.cuh", CSRC / "solver.cuh",
+            CSRC / "mkpp_device.cuh", GEN / f"{mech}.cuh", INCLUDE / "mkpp.h", Path(__file__)]
 
 
 def _stale(mech: str) -> bool:
@@ -99,8 +117,9 @@ def _link(mech: str, objs: list[Path]) -> Path:
 def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None = None) -> Path:
     """Compile the units of one mechanism in parallel and link the library."""
     LIB.mkdir(parents=True, exist_ok=True)
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda u: _compile_unit(mech, u, verbose), UNITS))
+    us = units(mech)
+    with ThreadPoolExecutor(max_workers=len(us)) as ex:
+        objs = list(ex.map(lambda u: _compile_unit(mech, u, verbose), us))
     return _link(mech, objs)
 
 

@@ -134,11 +134,14 @@ def _c_u64_array(c, name, values):
     c("};")
 
 
-def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots):
-    """Warp-cooperative form of one attempt: the same arithmetic, operation by
-    operation, as ``attempt``, with each tableau stage run as a static 32-lane
-    schedule (``warp_schedule``).  Used for the few cells whose step count
-    makes one lane too slow."""
+def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots):
+    """The stage programs of one attempt and the slot layout they use.
+
+    Each tableau stage of the attempt is one program of uniform operations
+    (``warp_schedule``), with the per-thread kernel's arithmetic, operation
+    by operation, in its order.  Slots beyond the per-thread layout (nslots):
+    the rates q_r, the Jacobian partials, and constants (-0, +0, 1,
+    1/(gamma h), c_ij/h, literals)."""
     v2l = plan.phys_to_var
     nr = len(plan.reactions)
     nq = max(nr, nv)
@@ -271,13 +274,66 @@ def _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots)
     sched = [warp_schedule.schedule(ops) for ops in progs]
     nconst = 4 + len(cterm_slot) + len(literals)
     const_vals = ["-0.0", "0.0", "1.0", "0.0"] + ["0.0"] * len(cterm_slot) + [_lit(v) for v in literals]
+    return {"progs": progs, "sched": sched, "npart": npart, "nq": nq, "Q": Q, "D": D, "CB": CB,
+            "nconst": nconst, "const_vals": const_vals, "literals": literals, "cterm_slot": cterm_slot,
+            "KT": Mech_KT, "total": CB + nconst}
 
+
+def _emit_table_attempt_head(c, coop, C):
+    """Head of the table-driven per-thread attempt (the increment and error
+    norm that follow are those of the unrolled attempt)."""
+    c("  // One Rosenbrock attempt of size h from the state in S[Y..], table-driven:")
+    c("  // one thread walks the stage programs of the cooperative kernel")
+    c("  // (coop::sched) on its own cell, step after step, the words of a step in")
+    c("  // order.  The operations of a step are independent, so the order changes")
+    c("  // no bit, and all lanes of a warp read the same word.  Returns the WRMS")
+    c("  // error norm and leaves the increment sum_j M_j K_j in S[DY..]; bit 1 of")
+    c("  // status is set on a zero pivot.")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static double attempt(SA& S, const KA& k, double h, int& status) {")
+    c("    for (int r = 0; r < NR; ++r) S[KT + r] = k(r);")
+    c("    for (int i = 0; i < NCONST; ++i) S[CB + i] = coop::const_val[i];")
+    c("    S[CB + 3] = 1.0 / (GAMMA * h);")
+    for (st, j), slot in coop["cterm_slot"].items():
+        cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+        c(f"    S[{slot}] = {_lit(cv)} / h;    // c{st}{j} / h")
+    c("    bool ok = true;")
+    c("    const int steps = coop::stage_step[NSTAGE];")
+    c("    for (int s = 0; s < steps; ++s) {")
+    c("      const unsigned long long* __restrict__ row = coop::sched + (size_t)s * 32;")
+    c("      for (int j = 0; j < 32; ++j) {")
+    c("        const unsigned long long w = __ldg(row + j);")
+    c("        const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);")
+    c("        const unsigned out = lo & 0xffffu;")
+    c("        if (out == 0xffffu) break;          // a step's idle lanes come last")
+    c("        if (hi >> 31) {")
+    c("          const double v = S[out];")
+    c("          ok = ok && (v != 0.0);")
+    c("          S[out] = 1.0 / v;")
+    c("        } else {")
+    c("          const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^")
+    c("                                                ((long long)(lo >> 31) << 63));")
+    c("          S[out] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
+    c("        }")
+    c("      }")
+    c("    }")
+    c("    if (!ok) status |= 1;")
+
+
+def _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY):
+    """Warp-cooperative form of one attempt: the stage programs of
+    ``_coop_build`` run as static 32-lane schedules.  Used for the few cells
+    whose step count makes one lane too slow, and (``table`` mechanisms) as
+    the table that the per-thread interpreter walks."""
+    progs, sched, npart, nq = coop["progs"], coop["sched"], coop["npart"], coop["nq"]
+    Q, D, CB, nconst = coop["Q"], coop["D"], coop["CB"], coop["nconst"]
+    const_vals, literals, cterm_slot, Mech_KT = coop["const_vals"], coop["literals"], coop["cterm_slot"], coop["KT"]
     c("")
     c("  // ---- warp-cooperative attempt (static warp schedules) ----")
     c(f"  static constexpr int NPART = {npart};")
-    c(f"  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm")
-    c(f"  static constexpr int D = NSLOTS + {nq};     // partial derivatives")
-    c(f"  static constexpr int CB = D + NPART;        // constants")
+    c(f"  static constexpr int Q = {Q};            // rates q_r, then q_i of the error norm")
+    c(f"  static constexpr int D = {D};     // partial derivatives")
+    c(f"  static constexpr int CB = {CB};        // constants")
     c(f"  static constexpr int NCONST = {nconst};")
     c(f"  static constexpr int COOP_SLOTS = CB + NCONST;")
     t = _Code()
@@ -604,7 +660,18 @@ def _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots):
     c("  }")
 
 
-def emit_mechanism(plan: ReducedPlan) -> str:
+# Above this many LU multiply-adds the per-thread attempt is table-driven
+# (TS1: 49299) instead of unrolled (SAPRC99: 9654, which already costs one to
+# two minutes of cicc + ptxas per kernel).
+TABLE_PRODUCTS = 20000
+
+
+def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
+    """Device header of one mechanism.  `table`: per-thread attempt walking
+    the cooperative stage programs instead of unrolled code (default: above
+    TABLE_PRODUCTS LU multiply-adds).  A table header has no adjoint."""
+    if table is None:
+        table = len(plan.products) > TABLE_PRODUCTS
     raw = plan.raw
     name = plan.name
     nv, ns, nr = plan.n_var, plan.n_species, len(plan.reactions)
@@ -710,7 +777,14 @@ def emit_mechanism(plan: ReducedPlan) -> str:
     c(f"  static constexpr int F = {FS};")
     c(f"  static constexpr int DY = {DY};")
     c(f"  static constexpr int KT = {KT};        // the cell's rate constants for the current host step")
-    c(f"  static constexpr int NSLOTS = {nslots};")
+    coop = _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots)
+    if table:
+        c("  // Table-driven attempt: the per-thread store holds all slots of the")
+        c("  // stage programs (rates, partials, constants).")
+        c(f"  static constexpr int NSLOTS = {coop['total']};")
+    else:
+        c(f"  static constexpr int NSLOTS = {nslots};")
+    c(f"  static constexpr bool TABLE_ATTEMPT = {'true' if table else 'false'};")
     c("")
     # ---------------- Fun
     used_y_f = sorted({v2l[s_] for r in plan.reactions for s_, _ in r.reactants})
@@ -795,6 +869,10 @@ def emit_mechanism(plan: ReducedPlan) -> str:
     c("  }")
     c("")
     # ---------------- LU factorization
+    # (Table mode: the unrolled factor, solve and attempt are not emitted.)
+    real_c = c
+    if table:
+        c = _Code()
     c("  // In-place row-wise Doolittle LU over the compact slots, in the operation")
     c("  // order of the reference plan.  The operands a row reuses (its own L")
     c("  // entries for the U part, the pivot column of U for the L part) are read")
@@ -909,6 +987,9 @@ def emit_mechanism(plan: ReducedPlan) -> str:
         c(f"      S[{kb} + i] = {expr};")
         c("    }")
         c(f"    solve(S, {kb});")
+    if table:
+        c = real_c
+        _emit_table_attempt_head(c, coop, C)
     c("    double err_sq = 0.0;")
     c("    #pragma unroll")
     c("    for (int i = 0; i < NV; ++i) {")
@@ -952,8 +1033,9 @@ def emit_mechanism(plan: ReducedPlan) -> str:
         c(f"    const double fac = 0.9 * pow(err, -{_lit(1.0 / elo)});")
     c("    return fmax(0.2, fmin(fac, 6.0));")
     c("  }")
-    _emit_coop(c, plan, nv, ns, stages, A, C, M, E, NewF, K0, Y, FS, DY, nslots)
-    _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots)
+    _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY)
+    if not table:
+        _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots)
     c("};")
     c("")
     c(f"}}  // namespace mkpp_{name}")

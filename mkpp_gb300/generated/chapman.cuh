@@ -242,6 +242,7 @@ struct Mech {
   static constexpr int DY = 24;
   static constexpr int KT = 27;        // the cell's rate constants for the current host step
   static constexpr int NSLOTS = 31;
+  static constexpr bool TABLE_ATTEMPT = false;
 
   // Mass-action tendencies F(y) of the variable species (logical order):
   // y(i) supplies the state, out(i, F_i) receives the result.
@@ -419,9 +420,9 @@ struct Mech {
 
   // ---- warp-cooperative attempt (static warp schedules) ----
   static constexpr int NPART = 6;
-  static constexpr int Q = NSLOTS;            // rates q_r, then q_i of the error norm
-  static constexpr int D = NSLOTS + 4;     // partial derivatives
-  static constexpr int CB = D + NPART;        // constants
+  static constexpr int Q = 31;            // rates q_r, then q_i of the error norm
+  static constexpr int D = 35;     // partial derivatives
+  static constexpr int CB = 41;        // constants
   static constexpr int NCONST = 9;
   static constexpr int COOP_SLOTS = CB + NCONST;
   // Run steps [s_begin, s_end) of the static warp schedule on S: one

@@ -23,12 +23,15 @@ def test_header_declares_reference_entry_points():
         assert name in syms
 
 
-def test_library_exports_every_declared_symbol():
+@pytest.mark.parametrize("mech", ["chapman", "ts1"])
+def test_library_exports_every_declared_symbol(mech):
+    """Unrolled (chapman) and table-driven (ts1, whose differentiation and
+    evaluation entries are stubs) libraries export the whole C ABI."""
     from mkpp_gb300 import build
     from mkpp_gb300.api import SIGNATURES
 
     try:
-        lib = build.build(("chapman",))[0]
+        lib = build.build((mech,))[0]
     except RuntimeError as e:  # no nvcc
         pytest.skip(str(e))
     out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True, check=True).stdout
@@ -39,4 +42,4 @@ def test_library_exports_every_declared_symbol():
     # loading resolves every symbol with ctypes (dlopen only; no CUDA call is made)
     from mkpp_gb300 import api
 
-    api.load_library("chapman")
+    api.load_library(mech)

@@ -34,9 +34,12 @@ from oracle.oracle import Oracle
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 MECHS = ["chapman", "small_strato", "saprc99"]
-# Step sizes of the oracle comparison: cond(W) at most ~10, 1.5e5 and 3e8.
-H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6}
-EXTREME = {"saprc99": (11, 32, 69)}
+# Step sizes of the oracle comparison: cond(W) at most ~10, 1.5e5, 3e8 and
+# (TS1, where a 1 s step already changes the state by O(1)) 2e10.
+H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6, "ts1": 1.0}
+# Rate constants of the shipped mechanisms that reach 1e29-1e41 1/s (Troe k0
+# evaluated as A exp(+C/T)); moderated to 1e3 as in the GPU forced-step test.
+EXTREME = {"saprc99": (11, 32, 69), "ts1": (375, 376, 383, 394, 397, 402)}
 
 
 @pytest.fixture(scope="module")
@@ -123,7 +126,14 @@ def test_per_thread_attempt_equals_cooperative_programs(hostsim, mech):
 
 @pytest.mark.parametrize("mech", MECHS)
 def test_per_thread_step_matches_oracle_with_forced_step(hostsim, mech):
-    lib = hostsim[mech]
+    _forced_step_vs_oracle(hostsim[mech], mech)
+
+
+def test_ts1_table_step_matches_oracle_with_forced_step(tmp_path):
+    _forced_step_vs_oracle(_compile(tmp_path, "ts1"), "ts1")
+
+
+def _forced_step_vs_oracle(lib, mech):
     L = _layout(lib)
     plan = load(mech)
     w, o, k, dk = _case(mech, 8)
@@ -144,3 +154,79 @@ def test_per_thread_step_matches_oracle_with_forced_step(hostsim, mech):
         ref = rep["conc"][plan.var_phys, 0]
         atol = np.array(o.raw["atol"])[plan.var_phys]
         assert np.all(np.abs(ynew - ref) <= 1e-9 * (np.abs(ref) + atol))
+
+
+def _compile(tmp, mech, include_first=None):
+    so = tmp / f"hostsim_{mech}_{'table' if include_first else 'unrolled'}.so"
+    inc = ([f"-I{include_first}"] if include_first else []) + [f"-I{ROOT / 'mkpp_gb300' / 'generated'}"]
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
+                    f"-I{HERE / 'hostsim'}", *inc, f"-I{ROOT / 'mkpp_gb300' / 'csrc'}",
+                    f'-DMKPP_MECH_HEADER="{mech}.cuh"', f"-DMKPP_MECH_NS=mkpp_{mech}",
+                    str(HERE / "hostsim" / "attempt_driver.cpp"), "-o", str(so)], check=True)
+    lib = C.CDLL(str(so))
+    lib.hostsim_attempt.restype = C.c_double
+    lib.hostsim_attempt.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_table_attempt_equals_unrolled_attempt(hostsim, mech, tmp_path):
+    """The table-driven per-thread attempt (emitted for mechanisms too large
+    to unroll, here forced) ends bit-identical to the unrolled one: state
+    increment, stage vectors, factorised LU and error norm."""
+    plan = load(mech)
+    (tmp_path / f"{mech}.cuh").write_text(cuda_emitter.emit_mechanism(plan, table=True))
+    table = _compile(tmp_path, mech, include_first=tmp_path)
+    unrolled = hostsim[mech]
+    Lt, Lu = _layout(table), _layout(unrolled)
+    assert Lt["NSLOTS"] > Lu["NSLOTS"] and all(Lt[k] == Lu[k] for k in ("Y", "K0", "F", "DY", "KT", "NV"))
+    w, o, k, _ = _case(mech)
+    nv = Lu["NV"]
+    for h in (1e-4, 10.0):
+        for c in range(w.ncells):
+            y = w.conc[plan.var_phys, c]
+            kc = np.ascontiguousarray(k[:, c])
+            out = []
+            for lib, L in ((unrolled, Lu), (table, Lt)):
+                S = np.zeros(L["NSLOTS"])
+                S[L["Y"]:L["Y"] + nv] = y
+                st = C.c_int(0)
+                err = lib.hostsim_attempt(S.ctypes.data, kc.ctypes.data, h, C.byref(st))
+                out.append((S[:L["KT"]].copy(), err, st.value))
+            assert np.array_equal(out[0][0], out[1][0])
+            assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
+
+
+def test_ts1_table_attempt_equals_its_programs(tmp_path):
+    """TS1 (210 species, 49299 LU multiply-adds) is emitted table-driven: its
+    host-compiled per-thread attempt gives the stage vectors and LU of its
+    stage programs executed in program order with exactly rounded fma."""
+    mech = "ts1"
+    lib = _compile(tmp_path, mech)
+    L = _layout(lib)
+    plan = load(mech)
+    cuda_emitter.emit_mechanism(plan)
+    progs, _, info = plan._coop_programs
+    w, o, k, _ = _case(mech, 1)
+    nv, nlu = L["NV"], len(plan.lu_slots)
+    h = 1e-4
+    y = np.ascontiguousarray(w.conc[plan.var_phys, 0])
+    kc = np.ascontiguousarray(k[:, 0])
+    S = np.zeros(L["NSLOTS"])
+    S[L["Y"]:L["Y"] + nv] = y
+    st = C.c_int(0)
+    lib.hostsim_attempt(S.ctypes.data, kc.ctypes.data, h, C.byref(st))
+    P = np.zeros(info["slots"])
+    P[info["Y"]:info["Y"] + nv] = y
+    P[info["KT"]:info["KT"] + len(kc)] = kc
+    CB = info["CB"]
+    P[CB:CB + 4] = (-0.0, 0.0, 1.0, 1.0 / (plan.tableau["Gamma"][0] * h))
+    for (s_, j), slot in info["cterm_slot"].items():
+        P[slot] = info["C"][(s_ - 1) * (s_ - 2) // 2 + j - 1] / h
+    for v, slot in info["literals"].items():
+        P[slot] = v
+    P = _run_programs(progs, P)
+    K = slice(L["K0"], L["K0"] + L["NSTAGE"] * nv)
+    assert np.isfinite(S[K]).all()
+    assert np.array_equal(S[K], P[K])
+    assert np.array_equal(S[:nlu], P[:nlu])
