@@ -176,31 +176,6 @@ def test_host_c_abi_matches_device_entry_points(built_libs):
     assert np.array_equal(host, conc.cpu().numpy())
 
 
-def test_launch_tuning_change_on_a_live_handle(built_libs):
-    """mkpp_integrate, then mkpp_set_launch_tuning to the 128-register variant
-    (twice the resident blocks, so a larger integrate scratch for SAPRC99's
-    global tile store), then mkpp_integrate again on the same handle and
-    inputs: the handle's scratch grows and the results are identical."""
-    from mkpp_gb300.api import MechanismContext
-
-    w, s, o = _setup("saprc99")
-    ctx = MechanismContext("saprc99", w.ncells)
-    outs = []
-    try:
-        for rv in (2, 4):
-            s.set_tuning(register_variant=rv)
-            host = np.ascontiguousarray(w.conc.copy())
-            ctx.set_state(host, w.temp.copy(), w.pressure.copy(), w.rho.copy())
-            ctx.set_aerosol(relative_humidity=w.rh.copy())
-            ctx.set_rate_parameters(np.ascontiguousarray(w.param))
-            ctx.integrate(w.dt)
-            outs.append(host.copy())
-    finally:
-        s.set_tuning(register_variant=2)
-        ctx.close()
-    assert np.array_equal(outs[0], outs[1], equal_nan=True)
-
-
 def test_steps_argument_equals_repeated_calls(built_libs):
     torch = _torch()
     w, s, o = _setup("small_strato")
