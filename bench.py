@@ -406,11 +406,7 @@ def main():
                            "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
                                                                      "one launch for all host steps")}
 
-    from mkpp_gb300.build import is_table
-
-    if rank == 0 and not args.no_adjoint and is_table(w.mechanism):
-        result["adjoint"] = {"unavailable": f"{w.mechanism} is table-driven: its library has no adjoint kernels"}
-    elif rank == 0 and not args.no_adjoint:
+    if rank == 0 and not args.no_adjoint:
         # Discrete adjoint (SAPRC99 adjoint configuration): first adjoint_cells
         # cells, one 3600 s integrate() with checkpoints at accepted steps, loss
         # sum_c (O3_c - O3t_c)^2 with O3t log-normal (sigma 0.2) around the

@@ -45,9 +45,9 @@ UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_capi.c
 
 
 # Units of a table-driven mechanism (too large to unroll, such as TS1): its
-# header has no adjoint, and the unrolled F/J evaluation kernels would take
-# minutes to compile, so the differentiation and evaluation entries are stubs.
-DIFF_UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_diff.cu", "mkpp_eval.cu")
+# unrolled F/J evaluation kernels would take minutes to compile, so the
+# evaluation entries are stubs.
+UNROLLED_ONLY = ("mkpp_eval.cu",)
 
 
 def is_table(mech: str) -> bool:
@@ -58,7 +58,7 @@ def is_table(mech: str) -> bool:
 
 def units(mech: str) -> tuple[str, ...]:
     if is_table(mech):
-        return tuple(u for u in UNITS if u not in DIFF_UNITS) + ("mkpp_diff_stub.cu", "mkpp_eval_stub.cu")
+        return tuple(u for u in UNITS if u not in UNROLLED_ONLY) + ("mkpp_eval_stub.cu",)
     return UNITS
 
 

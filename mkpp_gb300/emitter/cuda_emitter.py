@@ -134,7 +134,7 @@ def _c_u64_array(c, name, values):
     c("};")
 
 
-def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots):
+def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots, table=False, M=None):
     """The stage programs of one attempt and the slot layout they use.
 
     Each tableau stage of the attempt is one program of uniform operations
@@ -149,6 +149,17 @@ def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots):
     Q = nslots                      # rates q_r (then q_i of the error norm)
     D = nslots + nq                 # Jacobian partial derivatives
     CB = D + npart                  # constants: -0, +0, 1, 1/(gamma h), c_ij/h, literals
+    adj = None
+    if table:
+        # The table-driven adjoint's slots sit before the constants: lambda,
+        # the stage adjoints, the pending tendency adjoint, dL/dk, and
+        # temporaries (one per reaction, one per species, a few scalars).
+        adj = {"LAM": CB}
+        adj["KBAR"] = adj["LAM"] + nv
+        adj["FBAR"] = adj["KBAR"] + stages * nv
+        adj["KB"] = adj["FBAR"] + nv
+        adj["TMP"] = adj["KB"] + nr
+        CB = adj["TMP"] + nr + nv + 8
     ZN, ZP, ONE, IG = CB, CB + 1, CB + 2, CB + 3
     cterm_slot = {}
     for st in range(2, stages + 1):
@@ -272,11 +283,213 @@ def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots):
         P.solve(plan, kb)
         progs.append(P.ops)
     sched = [warp_schedule.schedule(ops) for ops in progs]
+    adj_ops = None
+    if table:
+        P = program()
+        _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, Mech_KT, adj, cterm_slot)
+        adj_ops = P.ops
     nconst = 4 + len(cterm_slot) + len(literals)
     const_vals = ["-0.0", "0.0", "1.0", "0.0"] + ["0.0"] * len(cterm_slot) + [_lit(v) for v in literals]
     return {"progs": progs, "sched": sched, "npart": npart, "nq": nq, "Q": Q, "D": D, "CB": CB,
             "nconst": nconst, "const_vals": const_vals, "literals": literals, "cterm_slot": cterm_slot,
-            "KT": Mech_KT, "total": CB + nconst}
+            "KT": Mech_KT, "total": CB + nconst, "adj": adj, "adj_ops": adj_ops}
+
+
+def _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, KT, adj, cterm_slot):
+    """The reverse of one accepted step as a sequential program: operation
+    for operation the arithmetic of the unrolled ``adjoint_step``
+    (``_emit_adjoint``), the same sums in the same order.  A term is a
+    product of factors evaluated left to right; a first term with a
+    coefficient c other than +-1 is c * f1 * f2 ... (c multiplied in first),
+    as the unrolled expressions associate."""
+    v2l = plan.phys_to_var
+    nr = len(plan.reactions)
+    LAM, KBAR, FBAR, KB, TMP = adj["LAM"], adj["KBAR"], adj["FBAR"], adj["KB"], adj["TMP"]
+    TS, TY = TMP, TMP + nr                       # per-reaction s, per-species stage state
+    T_S, T_G, T_KS, T_H, T_M, T_T, T_X = (TMP + nr + nv + i for i in range(7))
+
+    def product(dest, factors):
+        """dest = f1 * f2 * ... left to right (one factor: a copy)."""
+        if len(factors) == 1:
+            P.copy(dest, factors[0])
+            return
+        P.mul(dest, factors[0], factors[1])
+        for f in factors[2:]:
+            P.mul(dest, dest, f)
+
+    def mono(expo, ybase):
+        """Slot of prod y^e: the product is formed in T_M if it has more than
+        one factor.  Called just before the term that uses it."""
+        fac = [ybase(q) for q in sorted(expo) for _ in range(expo[q])]
+        if len(fac) == 1:
+            return fac[0]
+        product(T_M, fac)
+        return T_M
+
+    def accumulate(dest, terms):
+        """dest = sum over (coef, make) of coef * product(make()): first term
+        t, -t or c * f1 * f2 ..., then acc + t, acc - t or fma(c, t, acc)."""
+        for n_, (coef, make) in enumerate(terms):
+            factors = make()
+            if n_ == 0:
+                if coef == 1.0:
+                    product(dest, factors)
+                elif coef == -1.0:
+                    product(T_T, factors)
+                    P.fma(dest, T_T, P.one, P.zn, neg=True)
+                else:
+                    product(dest, [P.lit(coef)] + factors)
+            else:
+                product(T_T, factors)
+                if coef == 1.0:
+                    P.fma(dest, T_T, P.one, dest)
+                elif coef == -1.0:
+                    P.fma(dest, T_T, P.one, dest, neg=True)
+                else:
+                    P.fma(dest, P.lit(coef), T_T, dest)
+
+    def dot(net, base):
+        return [(float(co), (lambda i=i: [base + i])) for i, co in net]
+
+    def ymono_v(e2, vslot):
+        return lambda: ([mono(e2, lambda q: Y + q), vslot] if e2 else [vslot])
+
+    rx = [(r.index, _monomial_terms(r.reactants, v2l), [(v2l[s_], co) for s_, co in r.net]) for r in plan.reactions]
+    ucol = [[] for _ in range(nv)]
+    lcol = [[] for _ in range(nv)]
+    for (r_, cc), sl in plan.lu_index.items():
+        if r_ < cc:
+            ucol[cc].append((r_, sl))
+        elif r_ > cc:
+            lcol[cc].append((r_, sl))
+
+    def solve_t(base):
+        """W^T x = b in place: U^T forward (times 1/U_ii), then L^T backward."""
+        for i in range(nv):
+            for k_, sl in sorted(ucol[i]):
+                P.fma(base + i, sl, base + k_, base + i, neg=True)
+            P.mul(base + i, base + i, plan.diag[i])
+        for i in range(nv - 1, -1, -1):
+            for k_, sl in sorted(lcol[i]):
+                P.fma(base + i, sl, base + k_, base + i, neg=True)
+
+    def wterm(ub, vb):
+        """u^T J(y_n) v terms: dk into KB, Hessian-vector into LAM."""
+        for ri, expo, net in rx:
+            if not net or not expo:
+                continue
+            accumulate(T_S, dot(net, ub))
+            gterms = []
+            for j in sorted(expo):
+                coef, e2 = _dmono(expo, j)
+                gterms.append((coef, ymono_v(e2, vb + j)))
+            accumulate(T_G, gterms)
+            P.fma(KB + ri, T_S, T_G, KB + ri)
+            P.mul(T_KS, KT + ri, T_S)
+            for p_ in sorted(expo):
+                c1, e1 = _dmono(expo, p_)
+                hterms = []
+                for q in sorted(e1):
+                    c2, e2 = _dmono(e1, q)
+                    hterms.append((c1 * c2, ymono_v(e2, vb + q)))
+                if hterms:
+                    accumulate(T_H, hterms)
+                    P.fma(LAM + p_, T_KS, T_H, LAM + p_)
+
+    def fterm(yslot, aterms):
+        """Adjoint of F at the stage state: dk into KB, J^T Fbar into LAM and
+        the stage adjoints of the K_j the state is built from."""
+        for ri, expo, net in rx:
+            if not net:
+                continue
+            accumulate(TS + ri, dot(net, FBAR))
+            if expo:
+                P.fma(KB + ri, TS + ri, mono(expo, yslot), KB + ri)
+            else:
+                P.fma(KB + ri, TS + ri, P.one, KB + ri)
+        yb_terms = {j: [] for j in range(nv)}
+        for ri, expo, net in rx:
+            if not net:
+                continue
+            for j in sorted(expo):
+                coef, e2 = _dmono(expo, j)
+                fac = [KT + ri, TS + ri] + [yslot(q) for q in sorted(e2) for _ in range(e2[q])]
+                yb_terms[j].append((coef, (lambda fac=fac: fac)))
+        for j in range(nv):
+            if yb_terms[j]:
+                accumulate(T_X, yb_terms[j])
+                P.fma(LAM + j, T_X, P.one, LAM + j)
+                for a, jj in aterms:
+                    P.fma(KBAR + jj * nv + j, P.lit(a), T_X, KBAR + jj * nv + j)
+
+    for i in range(stages):
+        for j in range(nv):
+            if M[i] != 0.0:
+                P.mul(KBAR + i * nv + j, P.lit(M[i]), LAM + j)
+            else:
+                P.zero(KBAR + i * nv + j)
+    for j in range(nv):
+        P.zero(FBAR + j)
+    used = sorted({j for _, e, _ in rx for j in e})
+    for i in range(stages - 1, -1, -1):
+        kb = KBAR + i * nv
+        solve_t(kb)
+        wterm(kb, K0 + i * nv)
+        for j in range(nv):
+            P.fma(FBAR + j, kb + j, P.one, FBAR + j)
+        for j in range(i):
+            cv = C[i * (i - 1) // 2 + j]
+            if cv != 0.0:
+                slot = cterm_slot[(i + 1, j + 1)]
+                for q in range(nv):
+                    P.fma(KBAR + j * nv + q, slot, kb + q, KBAR + j * nv + q)
+        if NewF[i]:
+            aterms = [(A[i * (i - 1) // 2 + j], j) for j in range(i) if i > 0 and A[i * (i - 1) // 2 + j] != 0.0]
+            if aterms:
+                for q in used:
+                    acc = Y + q
+                    for a, j in aterms:
+                        kk = K0 + j * nv + q
+                        if a == 1.0:
+                            P.fma(TY + q, kk, P.one, acc)
+                        else:
+                            P.mul(T_T, kk, P.lit(a))
+                            P.fma(TY + q, T_T, P.one, acc)
+                        acc = TY + q
+                fterm(lambda q: TY + q, aterms)
+            else:
+                fterm(lambda q: Y + q, aterms)
+            for j in range(nv):
+                P.zero(FBAR + j)
+
+
+def _emit_table_adjoint(c, coop):
+    """Table-driven adjoint_step: one thread walks the reverse-step program
+    (``_adjoint_program``) on its own cell."""
+    adj = coop["adj"]
+    c("")
+    c("  // ---- discrete adjoint of one accepted step (table-driven) ----")
+    c(f"  static constexpr int LAM = {adj['LAM']};      // dL/dy")
+    c(f"  static constexpr int KBAR = {adj['KBAR']};    // stage adjoints, NSTAGE x NV")
+    c(f"  static constexpr int FBAR = {adj['FBAR']};    // adjoint of the pending stage tendency")
+    c(f"  static constexpr int KB = {adj['KB']};        // dL/dk accumulated")
+    c("  static constexpr int NSLOTS_ADJ = NSLOTS;")
+    c("  // Reverse of one accepted step of size h: walks coop::adj_prog, the")
+    c("  // arithmetic of the unrolled adjoint step operation by operation.")
+    c("  // Requires attempt() for this step first (LU, K_i, and the constants and")
+    c("  // rate constants it writes for h), y_n in S[Y..] and lambda in S[LAM..].")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static void adjoint_step(SA& S, const KA& k, double h) {")
+    c("    (void)k;")
+    c("    (void)h;")
+    c("    for (int n = 0; n < coop::ADJ_OPS; ++n) {")
+    c("      const unsigned long long w = __ldg(coop::adj_prog + n);")
+    c("      const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);")
+    c("      const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^")
+    c("                                            ((long long)(lo >> 31) << 63));")
+    c("      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
+    c("    }")
+    c("  }")
 
 
 def _emit_table_attempt_head(c, coop, C):
@@ -348,6 +561,10 @@ def _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY):
     for ops, st_ in zip(progs, sched):
         words += warp_schedule.encode(ops, st_)
     _c_u64_array(t, "sched", words)
+    if coop["adj_ops"] is not None:
+        ops = coop["adj_ops"]
+        t(f"constexpr int ADJ_OPS = {len(ops)};")
+        _c_u64_array(t, "adj_prog", warp_schedule.encode(ops, [[i] for i in range(len(ops))], lanes=1))
     t("}  // namespace coop")
     t("")
     plan._coop_tables = t.text()
@@ -667,9 +884,10 @@ TABLE_PRODUCTS = 20000
 
 
 def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
-    """Device header of one mechanism.  `table`: per-thread attempt walking
-    the cooperative stage programs instead of unrolled code (default: above
-    TABLE_PRODUCTS LU multiply-adds).  A table header has no adjoint."""
+    """Device header of one mechanism.  `table`: per-thread attempt and
+    adjoint step walking programs (the cooperative stage programs, the
+    reverse-step program) instead of unrolled code (default: above
+    TABLE_PRODUCTS LU multiply-adds)."""
     if table is None:
         table = len(plan.products) > TABLE_PRODUCTS
     raw = plan.raw
@@ -777,7 +995,7 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
     c(f"  static constexpr int F = {FS};")
     c(f"  static constexpr int DY = {DY};")
     c(f"  static constexpr int KT = {KT};        // the cell's rate constants for the current host step")
-    coop = _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots)
+    coop = _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots, table=table, M=M)
     if table:
         c("  // Table-driven attempt: the per-thread store holds all slots of the")
         c("  // stage programs (rates, partials, constants).")
@@ -1034,7 +1252,9 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
     c("    return fmax(0.2, fmin(fac, 6.0));")
     c("  }")
     _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY)
-    if not table:
+    if table:
+        _emit_table_adjoint(c, coop)
+    else:
         _emit_adjoint(c, plan, nv, nr, stages, A, C, M, NewF, K0, Y, nslots)
     c("};")
     c("")

@@ -1,5 +1,5 @@
-// One Rosenbrock attempt of an emitted mechanism header, on the host (TEST
-// INFRASTRUCTURE ONLY).  The store is a plain array of the per-cell slots
+// One Rosenbrock attempt, and the adjoint of one step, of an emitted mechanism
+// header on the host (TEST INFRASTRUCTURE ONLY).  The store is a plain array of the per-cell slots
 // (the layout of Mech: Y, stage vectors K0.., F, DY, KT), the rate constants
 // a plain array.
 #include MKPP_MECH_HEADER
@@ -33,6 +33,25 @@ double hostsim_attempt(double* slots, const double* k, double h, int* status) {
   const double err = Mech::attempt(S, Rates{k}, h, st);
   *status = st;
   return err;
+}
+
+// LAM, KB, NSLOTS_ADJ
+int hostsim_adj_layout(int* out) {
+  out[0] = Mech::LAM;
+  out[1] = Mech::KB;
+  out[2] = Mech::NSLOTS_ADJ;
+  return 0;
+}
+
+// The reverse of one step of size h, as the adjoint kernel runs it: the step
+// recomputed with attempt(), then adjoint_step() (lambda in S[LAM..] in,
+// dL/dy_n out; dL/dk added to S[KB..]).
+void hostsim_adjoint(double* slots, const double* k, double h, int* status) {
+  Store S{slots};
+  int st = 0;
+  Mech::attempt(S, Rates{k}, h, st);
+  Mech::adjoint_step(S, Rates{k}, h);
+  *status = st;
 }
 
 }  // extern "C"
