@@ -933,7 +933,9 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
     low, up = plan.solve_entries
     c(f"  static constexpr long long SOLVE_L = {low};")
     c(f"  static constexpr long long SOLVE_U = {up};")
-    # per-attempt algorithmic FP64 flop count (documented in the design doc)
+    # Algorithmic FP64 operations of F and of the Jacobian partials per
+    # evaluation (a multiply-add counts two); plan.flops_per_attempt adds
+    # the LU, solves, stages and error norm.
     fun_fl = sum(max(0, sum(pw for _, pw in r.reactants)) for r in plan.reactions) + \
         sum(2 * len(r.net) for r in plan.reactions)
     jac_fl = sum(2 * len(r.net) * len(r.reactants) for r in plan.reactions) + \
