@@ -414,12 +414,14 @@ def main():
         # rate constants.  Reported: adjoint time / checkpointed-forward time.
         from mkpp_gb300.adjoint import Checkpoints
 
-        na = min(n, args.adjoint_cells)
+        cap = 1536
+        # Checkpoints hold cap x NV doubles per cell: at most 100 GB of them
+        # (SAPRC99: 65536 cells = 63 GB; TS1 would need 168 GB for 65536).
+        na = min(n, args.adjoint_cells, int(100e9 // (cap * plan.n_var * 8)))
         ca0 = conc0[:, :na].contiguous()
         ka = ktab[0, :, :na].contiguous()
         del ktab
         torch.cuda.empty_cache()
-        cap = 1536
         ck = Checkpoints(w.mechanism, na, cap, dev)
         ev_f = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         ev_a = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
