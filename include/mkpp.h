@@ -194,6 +194,23 @@ int mkpp_gpu_adjoint(size_t num_cells, const double* ktab, int ckpt_cap, const d
                      double* grad_conc0, double* grad_k, void* workspace, size_t workspace_bytes,
                      void* stream);
 
+/* ---- Tangent (forward sensitivities; the reference's counterpart is
+ * SolverKernels::integrate_tlm, src/mkpp/templates/solver_variants/
+ * integrate_tlm.j2:32-215, a frozen-Jacobian tangent in the state alone;
+ * this one is the exact tangent of the accepted steps, the transpose of
+ * mkpp_gpu_adjoint, and also carries a direction in the rate constants) --- */
+/* Workspace of mkpp_gpu_tangent (per-thread scratch, 256-byte aligned). */
+size_t mkpp_gpu_tangent_workspace_bytes(size_t num_cells);
+/* Given the checkpoints of mkpp_gpu_integrate_checkpoint, a direction
+ * delta_conc0 in the starting state ([species][cells]; fixed species
+ * ignored) and delta_k in the rate constants ([reactions][cells], or NULL
+ * for none), writes delta_conc = d conc_end / d (conc0, k) applied to them
+ * ([species][cells]; fixed species 0) for the recorded step sequence. */
+int mkpp_gpu_tangent(size_t num_cells, const double* ktab, int ckpt_cap, const double* ckpt_y,
+                     const double* ckpt_h, const int* ckpt_n, const double* delta_conc0,
+                     const double* delta_k, double* delta_conc, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
 /* Allocation-free integrate (no counterpart in the reference).  For callers
  * that cannot allocate device memory at the point where they integrate: a
  * host model that records its time step into a CUDA graph (cudaMalloc is not

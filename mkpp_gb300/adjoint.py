@@ -1,5 +1,5 @@
 """Differentiable Rosenbrock solve: torch.autograd.Function over the GPU
-checkpointed forward and discrete-adjoint kernels.
+checkpointed forward, discrete-adjoint and tangent kernels.
 
     conc_end = rosenbrock_solve(conc0, ktab, "saprc99", dt=3600.0)
     loss = ((conc_end[o3] - target) ** 2).sum()
@@ -11,7 +11,14 @@ size of every accepted step; the backward sweeps them in reverse
 (``mkpp_gpu_adjoint``), recomputing each step's stages, and returns the exact
 gradient of the computed solution for that step sequence (the step sizes are
 treated as constants, as in any discrete adjoint of an adaptive method).
-Fixed species get a zero gradient: they enter only through ktab.
+
+Forward mode (``torch.autograd.forward_ad`` dual tensors) sweeps the same
+steps first to last (``mkpp_gpu_tangent``) and returns the directional
+derivative d conc_end (d conc0, d ktab), the transpose of the backward.
+
+integrate() leaves the fixed species as they are, so conc_end's fixed rows
+are conc0's: both directions pass those rows through unchanged.  Fixed
+species act on the variable ones only through ktab.
 """
 
 from __future__ import annotations
@@ -42,6 +49,7 @@ class Checkpoints:
         self.count = torch.zeros(ncells, dtype=torch.int32, device=device)
         ws = int(self.lib.mkpp_gpu_adjoint_workspace_bytes(C.c_size_t(ncells)))
         self.ws = torch.zeros(ws + 256, dtype=torch.uint8, device=device)
+        self.tws = None  # the tangent's workspace, allocated on first use
 
     def _stream(self):
         return C.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -66,6 +74,20 @@ class Checkpoints:
         if rc != MKPP_SUCCESS:
             raise MkppError(rc)
 
+    def tangent(self, ktab, dconc0, dk=None):
+        """d conc_end applied to (dconc0, dk) for the recorded steps (fixed
+        species 0)."""
+        if self.tws is None:
+            ws = int(self.lib.mkpp_gpu_tangent_workspace_bytes(C.c_size_t(self.n)))
+            self.tws = torch.zeros(ws + 256, dtype=torch.uint8, device=dconc0.device)
+        out = torch.empty((self.sizes.species, self.n), dtype=torch.float64, device=dconc0.device)
+        rc = self.lib.mkpp_gpu_tangent(
+            C.c_size_t(self.n), _p(ktab), C.c_int(self.cap), _p(self.y), _p(self.h), _p(self.count),
+            _p(dconc0), _p(dk), _p(out), _p(self.tws), C.c_size_t(self.tws.numel()), self._stream())
+        if rc != MKPP_SUCCESS:
+            raise MkppError(rc)
+        return out
+
     def adjoint(self, ktab, lam_end):
         gc = torch.empty((self.sizes.species, self.n), dtype=torch.float64, device=lam_end.device)
         gk = torch.empty((self.sizes.reactions, self.n), dtype=torch.float64, device=lam_end.device)
@@ -85,14 +107,34 @@ class RosenbrockSolve(torch.autograd.Function):
         ck = Checkpoints(mechanism, conc.shape[1], cap, conc.device)
         ck.forward(conc, k, dt, seed, max_attempts)
         ctx.ck = ck
+        ctx.k = k
+        ctx.fixed = _fixed_rows(mechanism, conc.device)
         ctx.save_for_backward(k)
         return conc
 
     @staticmethod
     def backward(ctx, grad_out):
         (k,) = ctx.saved_tensors
-        gc, gk = ctx.ck.adjoint(k, grad_out.contiguous())
+        g = grad_out.contiguous()
+        gc, gk = ctx.ck.adjoint(k, g)
+        gc[ctx.fixed] = g[ctx.fixed]
         return gc, gk, None, None, None, None, None
+
+    @staticmethod
+    def jvp(ctx, dconc0, dktab, *_):
+        k = ctx.k
+        if dconc0 is None:
+            dconc0 = torch.zeros((ctx.ck.sizes.species, ctx.ck.n), dtype=torch.float64, device=k.device)
+        d = dconc0.contiguous()
+        out = ctx.ck.tangent(k, d, None if dktab is None else dktab.contiguous())
+        out[ctx.fixed] = d[ctx.fixed]
+        return out
+
+
+def _fixed_rows(mechanism: str, device):
+    """Indices of the fixed species in the (species, cells) layout."""
+    fixed = load_raw(mechanism)["fixed"]
+    return torch.tensor([i for i, f in enumerate(fixed) if f], dtype=torch.long, device=device)
 
 
 def rosenbrock_solve(conc0, ktab, mechanism: str, dt: float, cap: int = 1280, seed: float | None = None,

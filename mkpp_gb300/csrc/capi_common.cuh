@@ -73,5 +73,8 @@ int launch_replay(const mkpp::LaunchArgs& a, const mkpp::CheckpointArgs& ck, dou
                   cudaStream_t stream);
 int launch_adjoint(const mkpp::AdjointArgs& a, const mkpp::CheckpointArgs& ck, double* scratch, int grid,
                    cudaStream_t stream);
+// mkpp_tangent.cu: forward sensitivities over the recorded steps.
+int launch_tangent(const mkpp::TangentArgs& a, const mkpp::CheckpointArgs& ck, double* scratch, int grid,
+                   cudaStream_t stream);
 
 }  // namespace mkpp_tu

@@ -614,4 +614,45 @@ __global__ void __launch_bounds__(kBlock, 2) adjoint_kernel(AdjointArgs a, Check
   }
 }
 
+struct TangentArgs {
+  int ncells;
+  const double* ktab;      // [NR][ncells]
+  const double* dconc0;    // [NS][ncells]  tangent of conc at the start (fixed species ignored)
+  const double* dk;        // [NR][ncells]  tangent of the rate constants, or null for none
+  double* dconc;           // [NS][ncells]  tangent of conc at the end (fixed species 0)
+};
+
+// Tangent sweep: for each accepted step, first to last, recompute the step
+// from its checkpoint with attempt() (bit-identical to the forward) and carry
+// the tangent through Mech::tlm_step.  tlm_step addresses the store through
+// its program's slot numbers, so the store is always the per-block tile.
+template <class Mech>
+__global__ void __launch_bounds__(kBlock, 2) tangent_kernel(TangentArgs a, CheckpointArgs ck, double* scratch) {
+  TileStore S{scratch + (size_t)blockIdx.x * Mech::NSLOTS_TLM * kBlock + threadIdx.x};
+  const size_t n = (size_t)a.ncells;
+  const size_t T = (size_t)gridDim.x * kBlock;
+  for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
+#pragma unroll 4
+    for (int r = 0; r < Mech::NR; ++r) {
+      S[Mech::KT + r] = __ldg(a.ktab + (size_t)r * n + c);
+      S[Mech::DKR + r] = a.dk ? __ldg(a.dk + (size_t)r * n + c) : 0.0;
+    }
+#pragma unroll 4
+    for (int i = 0; i < Mech::NV; ++i) S[Mech::DYT + i] = a.dconc0[c + n * Mech::var_phys(i)];
+    auto k = [&](int r) { return S[Mech::KT + r]; };
+    const int cnt = ck.n[c];
+    for (int s = 0; s < cnt; ++s) {
+#pragma unroll 4
+      for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] = ck.y[((size_t)s * Mech::NV + i) * n + c];
+      const double h = ck.h[(size_t)s * n + c];
+      int st = 0;
+      (void)Mech::attempt(S, k, h, st);
+      Mech::tlm_step(S, k, h);
+    }
+    for (int i = 0; i < Mech::NS; ++i) a.dconc[c + n * i] = 0.0;
+#pragma unroll 4
+    for (int i = 0; i < Mech::NV; ++i) a.dconc[c + n * Mech::var_phys(i)] = S[Mech::DYT + i];
+  }
+}
+
 }  // namespace mkpp

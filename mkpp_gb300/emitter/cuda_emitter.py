@@ -292,7 +292,7 @@ def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots, table=False
     const_vals = ["-0.0", "0.0", "1.0", "0.0"] + ["0.0"] * len(cterm_slot) + [_lit(v) for v in literals]
     return {"progs": progs, "sched": sched, "npart": npart, "nq": nq, "Q": Q, "D": D, "CB": CB,
             "nconst": nconst, "const_vals": const_vals, "literals": literals, "cterm_slot": cterm_slot,
-            "KT": Mech_KT, "total": CB + nconst, "adj": adj, "adj_ops": adj_ops}
+            "KT": Mech_KT, "total": CB + nconst, "adj": adj, "adj_ops": adj_ops, "A": A, "NewF": NewF}
 
 
 def _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, KT, adj, cterm_slot):
@@ -463,6 +463,173 @@ def _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, KT, adj, cterm_s
                 P.zero(FBAR + j)
 
 
+def _tlm_build(plan, nv, stages, A, C, M, NewF, K0, Y, KT, base):
+    """Tangent of one accepted step of size h (forward mode), as a sequential
+    program of uniform operations with its own slots and constants from
+    `base` on.  With W = I/(gamma h) - J(y) and F_i = f(Y_i):
+        dY_i = dy + sum_j a_ij dK_j
+        dF_i = J(Y_i) dY_i + sum_r net_r dk_r m_r(Y_i)       (NewF stages)
+        W dK_i = dF_i + sum_j c_ij/h dK_j + dJ K_i,
+        dJ K_i = sum_r net_r (dk_r grad m_r(y).K_i + k_r K_i^T H_r(y) dy)
+        dy_new = dy + sum_i M_i dK_i.
+    In: dy in DYT, dk in DKR (the rate constants' tangent); out: dy_new in
+    DYT.  The LU and the K_i are those attempt() left for this step."""
+    v2l = plan.phys_to_var
+    nr = len(plan.reactions)
+    L = {"DYT": base}
+    L["DKR"] = L["DYT"] + nv
+    L["DK"] = L["DKR"] + nr
+    L["DF"] = L["DK"] + stages * nv
+    L["TY"] = L["DF"] + nv
+    L["TD"] = L["TY"] + nv
+    TT = L["TD"] + nv
+    TCB = TT + 8
+    L["TCB"] = TCB
+    DYT, DKR, DK, DF, TY, TD = L["DYT"], L["DKR"], L["DK"], L["DF"], L["TY"], L["TD"]
+    T_A, T_B, T_P = TT, TT + 1, TT + 2
+    cterm = {}
+    for st in range(2, stages + 1):
+        for j in range(1, st):
+            if C[(st - 1) * (st - 2) // 2 + j - 1] != 0.0:
+                cterm[(st, j)] = TCB + 3 + len(cterm)
+    literals: dict[float, int] = {}
+    lit_base = TCB + 3 + len(cterm)
+
+    def lit(v):
+        v = float(v)
+        if v not in literals:
+            literals[v] = lit_base + len(literals)
+        return literals[v]
+
+    P = warp_schedule.Program(TCB, TCB + 1, TCB + 2, lit)
+
+    def product(dest, factors):
+        if not factors:
+            P.copy(dest, P.one)
+        elif len(factors) == 1:
+            P.copy(dest, factors[0])
+        else:
+            P.mul(dest, factors[0], factors[1])
+            for f in factors[2:]:
+                P.mul(dest, dest, f)
+
+    def add_scaled(dest, coef, src):
+        if coef == 1.0:
+            P.fma(dest, src, P.one, dest)
+        elif coef == -1.0:
+            P.fma(dest, src, P.one, dest, neg=True)
+        else:
+            P.fma(dest, lit(coef), src, dest)
+
+    def ys_of(expo, yslot):
+        return [yslot(q) for q in sorted(expo) for _ in range(expo[q])]
+
+    def grad_dot(dest, expo, yslot, vslot):
+        """dest = sum_j dm/dy_j (y) v_j"""
+        P.zero(dest)
+        for j in sorted(expo):
+            c1, e2 = _dmono(expo, j)
+            product(T_P, ys_of(e2, yslot) + [vslot(j)])
+            add_scaled(dest, c1, T_P)
+
+    def hess(dest, expo, yslot, uslot, vslot):
+        """dest = sum_p sum_q u_p d2m/dy_p dy_q (y) v_q"""
+        P.zero(dest)
+        for p_ in sorted(expo):
+            c1, e1 = _dmono(expo, p_)
+            for q in sorted(e1):
+                c2, e2 = _dmono(e1, q)
+                product(T_P, ys_of(e2, yslot) + [uslot(p_), vslot(q)])
+                add_scaled(dest, c1 * c2, T_P)
+
+    rx = [(r.index, _monomial_terms(r.reactants, v2l), [(v2l[s_], co) for s_, co in r.net]) for r in plan.reactions]
+    for i in range(stages):
+        kb = DK + i * nv
+        if NewF[i]:
+            aterms = [(A[i * (i - 1) // 2 + j], j) for j in range(i) if i > 0 and A[i * (i - 1) // 2 + j] != 0.0]
+            if aterms:
+                for q in range(nv):
+                    P.copy(TY + q, Y + q)
+                    P.copy(TD + q, DYT + q)
+                    for a_, j in aterms:
+                        add_scaled(TY + q, a_, K0 + j * nv + q)
+                        add_scaled(TD + q, a_, DK + j * nv + q)
+                ys, ds = (lambda q: TY + q), (lambda q: TD + q)
+            else:
+                ys, ds = (lambda q: Y + q), (lambda q: DYT + q)
+            for q in range(nv):
+                P.zero(DF + q)
+            for ri, expo, net in rx:
+                if not net:
+                    continue
+                if expo:
+                    grad_dot(T_A, expo, ys, ds)
+                    P.mul(T_A, KT + ri, T_A)
+                else:
+                    P.zero(T_A)
+                product(T_B, ys_of(expo, ys))
+                P.fma(T_A, DKR + ri, T_B, T_A)
+                for p_, co in net:
+                    add_scaled(DF + p_, float(co), T_A)
+        for q in range(nv):
+            P.copy(kb + q, DF + q)
+            for j in range(i):
+                if (i + 1, j + 1) in cterm:
+                    P.fma(kb + q, cterm[(i + 1, j + 1)], DK + j * nv + q, kb + q)
+        for ri, expo, net in rx:
+            if not net or not expo:
+                continue
+            grad_dot(T_A, expo, lambda q: Y + q, lambda q, i=i: K0 + i * nv + q)
+            P.mul(T_A, DKR + ri, T_A)
+            hess(T_B, expo, lambda q: Y + q, lambda p_, i=i: K0 + i * nv + p_, lambda q: DYT + q)
+            P.fma(T_A, KT + ri, T_B, T_A)
+            for p_, co in net:
+                add_scaled(kb + p_, float(co), T_A)
+        P.solve(plan, kb)
+    for q in range(nv):
+        for i in range(stages):
+            if M[i] != 0.0:
+                add_scaled(DYT + q, M[i], DK + i * nv + q)
+    nconst = 3 + len(cterm) + len(literals)
+    const_vals = ["-0.0", "0.0", "1.0"] + ["0.0"] * len(cterm) + [_lit(v) for v in literals]
+    return {"ops": P.ops, "L": L, "cterm": cterm, "nconst": nconst, "const_vals": const_vals,
+            "total": TCB + nconst}
+
+
+def _emit_tlm(c, t, tlm, C):
+    """Constants, tables (into the coop namespace text t) and tlm_step."""
+    L = tlm["L"]
+    ops = tlm["ops"]
+    t(f"constexpr int TLM_OPS = {len(ops)};")
+    t(f"static __device__ const double tlm_const_val[{tlm['nconst']}] = {{{', '.join(tlm['const_vals'])}}};")
+    _c_u64_array(t, "tlm_prog", warp_schedule.encode(ops, [[i] for i in range(len(ops))], lanes=1))
+    c("")
+    c("  // ---- tangent of one accepted step (forward sensitivities) ----")
+    c(f"  static constexpr int DYT = {L['DYT']};     // dy in, dy_new out (NV)")
+    c(f"  static constexpr int DKR = {L['DKR']};     // dk, the rate constants' tangent (NR)")
+    c(f"  static constexpr int TLM_CB = {L['TCB']};  // constants of the tangent program")
+    c(f"  static constexpr int TLM_NCONST = {tlm['nconst']};")
+    c(f"  static constexpr int NSLOTS_TLM = {tlm['total']};")
+    c("  // dy_new = d(y_new)/d(y, k) (dy, dk) for one step of size h: walks")
+    c("  // coop::tlm_prog.  Requires attempt() for this step first (the LU of W and")
+    c("  // the K_i), y_n in S[Y..], dy in S[DYT..] and dk in S[DKR..].")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static void tlm_step(SA& S, const KA& k, double h) {")
+    c("    for (int r = 0; r < NR; ++r) S[KT + r] = k(r);")
+    c("    for (int i = 0; i < TLM_NCONST; ++i) S[TLM_CB + i] = coop::tlm_const_val[i];")
+    for (st, j), slot in tlm["cterm"].items():
+        cv = C[(st - 1) * (st - 2) // 2 + j - 1]
+        c(f"    S[{slot}] = {_lit(cv)} / h;    // c{st}{j} / h")
+    c("    for (int n = 0; n < coop::TLM_OPS; ++n) {")
+    c("      const unsigned long long w = __ldg(coop::tlm_prog + n);")
+    c("      const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);")
+    c("      const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^")
+    c("                                            ((long long)(lo >> 31) << 63));")
+    c("      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
+    c("    }")
+    c("  }")
+
+
 def _emit_table_adjoint(c, coop):
     """Table-driven adjoint_step: one thread walks the reverse-step program
     (``_adjoint_program``) on its own cell."""
@@ -565,6 +732,10 @@ def _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY):
         ops = coop["adj_ops"]
         t(f"constexpr int ADJ_OPS = {len(ops)};")
         _c_u64_array(t, "adj_prog", warp_schedule.encode(ops, [[i] for i in range(len(ops))], lanes=1))
+    tlm = _tlm_build(plan, nv, stages, coop["A"], C, M, coop["NewF"], K0, Y, Mech_KT, coop["total"])
+    tlm_code = _Code()
+    _emit_tlm(tlm_code, t, tlm, C)
+    plan._tlm = tlm
     t("}  // namespace coop")
     t("")
     plan._coop_tables = t.text()
@@ -674,6 +845,8 @@ def _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY):
     c("    }")
     c("    return __shfl_sync(0xffffffffu, err, 0);")
     c("  }")
+    for line in tlm_code.lines:
+        c(line)
 
 
 def _monomial_terms(reactants, v2l):

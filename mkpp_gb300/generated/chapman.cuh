@@ -183,6 +183,47 @@ static __device__ const unsigned long long sched[1376] = {
     0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
     0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
 };
+constexpr int TLM_OPS = 291;
+static __device__ const double tlm_const_val[9] = {-0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 2.0, 6.1697947043828245, -0.42772256543218573};
+static __device__ const unsigned long long tlm_prog[291] = {
+    0x54005400540042ull, 0x54005400540043ull, 0x54005400540044ull, 0x5400540054004bull, 0x5300550034004dull, 0x4b0055004d004bull, 0x53004b001b004bull, 0x530055000b004cull,
+    0x4b004c0035004bull, 0x440055804b0044ull, 0x43004b00590043ull, 0x5400540054004bull, 0x530033000b004dull, 0x4b0055004d004bull, 0x530034000a004dull, 0x4b0055004d004bull,
+    0x53004b001c004bull, 0x53000b000a004cull, 0x4b004c0036004bull, 0x430055804b0043ull, 0x440055804b0044ull, 0x420055004b0042ull, 0x5400540054004bull, 0x5300550032004dull,
+    0x4b0055004d004bull, 0x53004b001d004bull, 0x5300550009004cull, 0x4b004c0037004bull, 0x420055804b0042ull, 0x430055004b0043ull, 0x440055004b0044ull, 0x5400540054004bull,
+    0x530032000a004dull, 0x4b0055004d004bull, 0x5300330009004dull, 0x4b0055004d004bull, 0x53004b001e004bull, 0x53000a0009004cull, 0x4b004c0038004bull, 0x430055804b0043ull,
+    0x420055804b0042ull, 0x44004b00590044ull, 0x53005500420039ull, 0x5300550043003aull, 0x5300550044003bull, 0x5400540054004bull, 0x530055000e004dull, 0x4b0055004d004bull,
+    0x53004b0035004bull, 0x5400540054004cull, 0x4b004c001b004bull, 0x3b0055804b003bull, 0x3a004b0059003aull, 0x5400540054004bull, 0x53000d000b004dull, 0x4b0055004d004bull,
+    0x53000e000a004dull, 0x4b0055004d004bull, 0x53004b0036004bull, 0x5400540054004cull, 0x530034000d004dull, 0x4c0055004d004cull, 0x530033000e004dull, 0x4c0055004d004cull,
+    0x4b004c001c004bull, 0x3a0055804b003aull, 0x3b0055804b003bull, 0x390055004b0039ull, 0x5400540054004bull, 0x530055000c004dull, 0x4b0055004d004bull, 0x53004b0037004bull,
+    0x5400540054004cull, 0x4b004c001d004bull, 0x390055804b0039ull, 0x3a0055004b003aull, 0x3b0055004b003bull, 0x5400540054004bull, 0x53000c000a004dull, 0x4b0055004d004bull,
+    0x53000d0009004dull, 0x4b0055004d004bull, 0x53004b0038004bull, 0x5400540054004cull, 0x530033000c004dull, 0x4c0055004d004cull, 0x530032000d004dull, 0x4c0055004d004cull,
+    0x4b004c001e004bull, 0x3a0055804b003aull, 0x390055804b0039ull, 0x3b004b0059003bull, 0x3a00398003003aull, 0x3b00398006003bull, 0x3b003a8007003bull, 0x530008003b003bull,
+    0x3a003b8005003aull, 0x530004003a003aull, 0x39003a80010039ull, 0x39003b80020039ull, 0x53000000390039ull, 0x53005500090045ull, 0x53005500320048ull, 0x450055000c0045ull,
+    0x48005500390048ull, 0x530055000a0046ull, 0x53005500330049ull, 0x460055000d0046ull, 0x490055003a0049ull, 0x530055000b0047ull, 0x5300550034004aull, 0x470055000e0047ull,
+    0x4a0055003b004aull, 0x54005400540042ull, 0x54005400540043ull, 0x54005400540044ull, 0x5400540054004bull, 0x530055004a004dull, 0x4b0055004d004bull, 0x53004b001b004bull,
+    0x5300550047004cull, 0x4b004c0035004bull, 0x440055804b0044ull, 0x43004b00590043ull, 0x5400540054004bull, 0x5300490047004dull, 0x4b0055004d004bull, 0x53004a0046004dull,
+    0x4b0055004d004bull, 0x53004b001c004bull, 0x5300470046004cull, 0x4b004c0036004bull, 0x430055804b0043ull, 0x440055804b0044ull, 0x420055004b0042ull, 0x5400540054004bull,
+    0x5300550048004dull, 0x4b0055004d004bull, 0x53004b001d004bull, 0x5300550045004cull, 0x4b004c0037004bull, 0x420055804b0042ull, 0x430055004b0043ull, 0x440055004b0044ull,
+    0x5400540054004bull, 0x5300480046004dull, 0x4b0055004d004bull, 0x5300490045004dull, 0x4b0055004d004bull, 0x53004b001e004bull, 0x5300460045004cull, 0x4b004c0038004bull,
+    0x430055804b0043ull, 0x420055804b0042ull, 0x44004b00590044ull, 0x5300550042003cull, 0x3c00390056003cull, 0x5300550043003dull, 0x3d003a0056003dull, 0x5300550044003eull,
+    0x3e003b0056003eull, 0x5400540054004bull, 0x5300550011004dull, 0x4b0055004d004bull, 0x53004b0035004bull, 0x5400540054004cull, 0x4b004c001b004bull, 0x3e0055804b003eull,
+    0x3d004b0059003dull, 0x5400540054004bull, 0x530010000b004dull, 0x4b0055004d004bull, 0x530011000a004dull, 0x4b0055004d004bull, 0x53004b0036004bull, 0x5400540054004cull,
+    0x5300340010004dull, 0x4c0055004d004cull, 0x5300330011004dull, 0x4c0055004d004cull, 0x4b004c001c004bull, 0x3d0055804b003dull, 0x3e0055804b003eull, 0x3c0055004b003cull,
+    0x5400540054004bull, 0x530055000f004dull, 0x4b0055004d004bull, 0x53004b0037004bull, 0x5400540054004cull, 0x4b004c001d004bull, 0x3c0055804b003cull, 0x3d0055004b003dull,
+    0x3e0055004b003eull, 0x5400540054004bull, 0x53000f000a004dull, 0x4b0055004d004bull, 0x5300100009004dull, 0x4b0055004d004bull, 0x53004b0038004bull, 0x5400540054004cull,
+    0x530033000f004dull, 0x4c0055004d004cull, 0x5300320010004dull, 0x4c0055004d004cull, 0x4b004c001e004bull, 0x3d0055804b003dull, 0x3c0055804b003cull, 0x3e004b0059003eull,
+    0x3d003c8003003dull, 0x3e003c8006003eull, 0x3e003d8007003eull, 0x530008003e003eull, 0x3d003e8005003dull, 0x530004003d003dull, 0x3c003d8001003cull, 0x3c003e8002003cull,
+    0x530000003c003cull, 0x5300550042003full, 0x3f00390057003full, 0x3f003c0058003full, 0x53005500430040ull, 0x40003a00570040ull, 0x40003d00580040ull, 0x53005500440041ull,
+    0x41003b00570041ull, 0x41003e00580041ull, 0x5400540054004bull, 0x5300550014004dull, 0x4b0055004d004bull, 0x53004b0035004bull, 0x5400540054004cull, 0x4b004c001b004bull,
+    0x410055804b0041ull, 0x40004b00590040ull, 0x5400540054004bull, 0x530013000b004dull, 0x4b0055004d004bull, 0x530014000a004dull, 0x4b0055004d004bull, 0x53004b0036004bull,
+    0x5400540054004cull, 0x5300340013004dull, 0x4c0055004d004cull, 0x5300330014004dull, 0x4c0055004d004cull, 0x4b004c001c004bull, 0x400055804b0040ull, 0x410055804b0041ull,
+    0x3f0055004b003full, 0x5400540054004bull, 0x5300550012004dull, 0x4b0055004d004bull, 0x53004b0037004bull, 0x5400540054004cull, 0x4b004c001d004bull, 0x3f0055804b003full,
+    0x400055004b0040ull, 0x410055004b0041ull, 0x5400540054004bull, 0x530012000a004dull, 0x4b0055004d004bull, 0x5300130009004dull, 0x4b0055004d004bull, 0x53004b0038004bull,
+    0x5400540054004cull, 0x5300330012004dull, 0x4c0055004d004cull, 0x5300320013004dull, 0x4c0055004d004cull, 0x4b004c001e004bull, 0x400055804b0040ull, 0x3f0055804b003full,
+    0x41004b00590041ull, 0x40003f80030040ull, 0x41003f80060041ull, 0x41004080070041ull, 0x53000800410041ull, 0x40004180050040ull, 0x53000400400040ull, 0x3f00408001003full,
+    0x3f00418002003full, 0x530000003f003full, 0x32005500390032ull, 0x32003c005a0032ull, 0x32003f005b0032ull, 0x330055003a0033ull, 0x33003d005a0033ull, 0x330040005b0033ull,
+    0x340055003b0034ull, 0x34003e005a0034ull, 0x340041005b0034ull,
+};
 }  // namespace coop
 
 
@@ -513,6 +554,31 @@ struct Mech {
       err = fmax(sqrt(err_sq / 4.0), 1.0e-10);
     }
     return __shfl_sync(0xffffffffu, err, 0);
+  }
+
+  // ---- tangent of one accepted step (forward sensitivities) ----
+  static constexpr int DYT = 50;     // dy in, dy_new out (NV)
+  static constexpr int DKR = 53;     // dk, the rate constants' tangent (NR)
+  static constexpr int TLM_CB = 83;  // constants of the tangent program
+  static constexpr int TLM_NCONST = 9;
+  static constexpr int NSLOTS_TLM = 92;
+  // dy_new = d(y_new)/d(y, k) (dy, dk) for one step of size h: walks
+  // coop::tlm_prog.  Requires attempt() for this step first (the LU of W and
+  // the K_i), y_n in S[Y..], dy in S[DYT..] and dk in S[DKR..].
+  template <class SA, class KA>
+  __device__ __forceinline__ static void tlm_step(SA& S, const KA& k, double h) {
+    for (int r = 0; r < NR; ++r) S[KT + r] = k(r);
+    for (int i = 0; i < TLM_NCONST; ++i) S[TLM_CB + i] = coop::tlm_const_val[i];
+    S[86] = -1.0156171083877703 / h;    // c21 / h
+    S[87] = 4.0759956452537702 / h;    // c31 / h
+    S[88] = 9.20767942983308 / h;    // c32 / h
+    for (int n = 0; n < coop::TLM_OPS; ++n) {
+      const unsigned long long w = __ldg(coop::tlm_prog + n);
+      const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+      const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^
+                                            ((long long)(lo >> 31) << 63));
+      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);
+    }
   }
 
   // ---- discrete adjoint of one accepted step ----

@@ -347,6 +347,103 @@ static __device__ const unsigned long long sched[2688] = {
     0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
     0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull, 0xffffull,
 };
+constexpr int TLM_OPS = 737;
+static __device__ const double tlm_const_val[9] = {-0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 2.0, 6.1697947043828245, -0.42772256543218573};
+static __device__ const unsigned long long tlm_prog[737] = {
+    0xaa00aa00aa008full, 0xaa00aa00aa0090ull, 0xaa00aa00aa0091ull, 0xaa00aa00aa0092ull, 0xaa00aa00aa0093ull, 0xaa00aa00aa0094ull, 0xaa00aa00aa00a1ull, 0xa900ab006f00a3ull,
+    0xa100ab00a300a1ull, 0xa900a1004100a1ull, 0xa900ab001f00a2ull, 0xa100a2007300a1ull, 0x9100ab80a10091ull, 0x9000a100af0090ull, 0xaa00aa00aa00a1ull, 0xa9006e001f00a3ull,
+    0xa100ab00a300a1ull, 0xa9006f001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1004200a1ull, 0xa9001f001e00a2ull, 0xa100a2007400a1ull, 0x9000ab80a10090ull, 0x9100ab80a10091ull,
+    0x9200ab00a10092ull, 0xaa00aa00aa00a1ull, 0xa900ab007000a3ull, 0xa100ab00a300a1ull, 0xa900a1004300a1ull, 0xa900ab002000a2ull, 0xa100a2007500a1ull, 0x9200ab80a10092ull,
+    0x9000ab00a10090ull, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa9006e002000a3ull, 0xa100ab00a300a1ull, 0xa90070001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1004400a1ull,
+    0xa90020001e00a2ull, 0xa100a2007600a1ull, 0x9000ab80a10090ull, 0x9200ab80a10092ull, 0x9100a100af0091ull, 0xaa00aa00aa00a1ull, 0xa900ab007000a3ull, 0xa100ab00a300a1ull,
+    0xa900a1004500a1ull, 0xa900ab002000a2ull, 0xa100a2007700a1ull, 0x9200ab80a10092ull, 0x8f00ab00a1008full, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa900ab006d00a3ull,
+    0xa100ab00a300a1ull, 0xa900a1004600a1ull, 0xa900ab001d00a2ull, 0xa100a2007800a1ull, 0x8f00ab80a1008full, 0x9000ab00a10090ull, 0xaa00aa00aa00a1ull, 0xa9006d002000a3ull,
+    0xa100ab00a300a1ull, 0xa90070001d00a3ull, 0xa100ab00a300a1ull, 0xa900a1004700a1ull, 0xa90020001d00a2ull, 0xa100a2007900a1ull, 0x8f00ab80a1008full, 0x9200ab80a10092ull,
+    0x9100a100af0091ull, 0xaa00aa00aa00a1ull, 0xa90070002100a3ull, 0xa100ab00a300a1ull, 0xa90071002000a3ull, 0xa100ab00a300a1ull, 0xa900a1004800a1ull, 0xa90021002000a2ull,
+    0xa100a2007a00a1ull, 0x9300ab80a10093ull, 0x9200ab80a10092ull, 0x9400ab00a10094ull, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa9006e002200a3ull, 0xa100ab00a300a1ull,
+    0xa90072001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1004900a1ull, 0xa90022001e00a2ull, 0xa100a2007b00a1ull, 0x9400ab80a10094ull, 0x9000ab80a10090ull, 0x9300ab00a10093ull,
+    0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa900ab007200a3ull, 0xa100ab00a300a1ull, 0xa900a1004a00a1ull, 0xa900ab002200a2ull, 0xa100a2007c00a1ull, 0x9400ab80a10094ull,
+    0x9300ab00a10093ull, 0x9000ab00a10090ull, 0xa900ab008f007dull, 0xa900ab0090007eull, 0xa900ab0091007full, 0xa900ab00920080ull, 0xa900ab00930081ull, 0xa900ab00940082ull,
+    0xaa00aa00aa00a1ull, 0xa900ab002500a3ull, 0xa100ab00a300a1ull, 0xa900a1007300a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004100a1ull, 0x7f00ab80a1007full, 0x7e00a100af007eull,
+    0xaa00aa00aa00a1ull, 0xa90024001f00a3ull, 0xa100ab00a300a1ull, 0xa90025001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007400a1ull, 0xaa00aa00aa00a2ull, 0xa9006f002400a3ull,
+    0xa200ab00a300a2ull, 0xa9006e002500a3ull, 0xa200ab00a300a2ull, 0xa100a2004200a1ull, 0x7e00ab80a1007eull, 0x7f00ab80a1007full, 0x8000ab00a10080ull, 0xaa00aa00aa00a1ull,
+    0xa900ab002600a3ull, 0xa100ab00a300a1ull, 0xa900a1007500a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004300a1ull, 0x8000ab80a10080ull, 0x7e00ab00a1007eull, 0x7f00ab00a1007full,
+    0xaa00aa00aa00a1ull, 0xa90024002000a3ull, 0xa100ab00a300a1ull, 0xa90026001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007600a1ull, 0xaa00aa00aa00a2ull, 0xa90070002400a3ull,
+    0xa200ab00a300a2ull, 0xa9006e002600a3ull, 0xa200ab00a300a2ull, 0xa100a2004400a1ull, 0x7e00ab80a1007eull, 0x8000ab80a10080ull, 0x7f00a100af007full, 0xaa00aa00aa00a1ull,
+    0xa900ab002600a3ull, 0xa100ab00a300a1ull, 0xa900a1007700a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004500a1ull, 0x8000ab80a10080ull, 0x7d00ab00a1007dull, 0x7f00ab00a1007full,
+    0xaa00aa00aa00a1ull, 0xa900ab002300a3ull, 0xa100ab00a300a1ull, 0xa900a1007800a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004600a1ull, 0x7d00ab80a1007dull, 0x7e00ab00a1007eull,
+    0xaa00aa00aa00a1ull, 0xa90023002000a3ull, 0xa100ab00a300a1ull, 0xa90026001d00a3ull, 0xa100ab00a300a1ull, 0xa900a1007900a1ull, 0xaa00aa00aa00a2ull, 0xa90070002300a3ull,
+    0xa200ab00a300a2ull, 0xa9006d002600a3ull, 0xa200ab00a300a2ull, 0xa100a2004700a1ull, 0x7d00ab80a1007dull, 0x8000ab80a10080ull, 0x7f00a100af007full, 0xaa00aa00aa00a1ull,
+    0xa90026002100a3ull, 0xa100ab00a300a1ull, 0xa90027002000a3ull, 0xa100ab00a300a1ull, 0xa900a1007a00a1ull, 0xaa00aa00aa00a2ull, 0xa90071002600a3ull, 0xa200ab00a300a2ull,
+    0xa90070002700a3ull, 0xa200ab00a300a2ull, 0xa100a2004800a1ull, 0x8100ab80a10081ull, 0x8000ab80a10080ull, 0x8200ab00a10082ull, 0x7f00ab00a1007full, 0xaa00aa00aa00a1ull,
+    0xa90024002200a3ull, 0xa100ab00a300a1ull, 0xa90028001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007b00a1ull, 0xaa00aa00aa00a2ull, 0xa90072002400a3ull, 0xa200ab00a300a2ull,
+    0xa9006e002800a3ull, 0xa200ab00a300a2ull, 0xa100a2004900a1ull, 0x8200ab80a10082ull, 0x7e00ab80a1007eull, 0x8100ab00a10081ull, 0x7f00ab00a1007full, 0xaa00aa00aa00a1ull,
+    0xa900ab002800a3ull, 0xa100ab00a300a1ull, 0xa900a1007c00a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004a00a1ull, 0x8200ab80a10082ull, 0x8100ab00a10081ull, 0x7e00ab00a1007eull,
+    0x7e007d8002007eull, 0x7f007d8007007full, 0x7f007e8008007full, 0x80007d800d0080ull, 0x80007e800e0080ull, 0x80007f800f0080ull, 0x81007e80130081ull, 0x81007f80140081ull,
+    0x81008080150081ull, 0x82007e80180082ull, 0x82007f80190082ull, 0x820080801a0082ull, 0x820081801b0082ull, 0xa9001c00820082ull, 0x81008280170081ull, 0xa9001600810081ull,
+    0x80008180110080ull, 0x80008280120080ull, 0xa9001000800080ull, 0x7f0080800a007full, 0x7f0081800b007full, 0x7f0082800c007full, 0xa90009007f007full, 0x7e007f8004007eull,
+    0x7e00808005007eull, 0x7e00828006007eull, 0xa90003007e007eull, 0x7d00808001007dull, 0xa90000007d007dull, 0xa900ab001d0095ull, 0xa900ab006d009bull, 0x9500ab00230095ull,
+    0x9b00ab007d009bull, 0xa900ab001e0096ull, 0xa900ab006e009cull, 0x9600ab00240096ull, 0x9c00ab007e009cull, 0xa900ab001f0097ull, 0xa900ab006f009dull, 0x9700ab00250097ull,
+    0x9d00ab007f009dull, 0xa900ab00200098ull, 0xa900ab0070009eull, 0x9800ab00260098ull, 0x9e00ab0080009eull, 0xa900ab00210099ull, 0xa900ab0071009full, 0x9900ab00270099ull,
+    0x9f00ab0081009full, 0xa900ab0022009aull, 0xa900ab007200a0ull, 0x9a00ab0028009aull, 0xa000ab008200a0ull, 0xaa00aa00aa008full, 0xaa00aa00aa0090ull, 0xaa00aa00aa0091ull,
+    0xaa00aa00aa0092ull, 0xaa00aa00aa0093ull, 0xaa00aa00aa0094ull, 0xaa00aa00aa00a1ull, 0xa900ab009d00a3ull, 0xa100ab00a300a1ull, 0xa900a1004100a1ull, 0xa900ab009700a2ull,
+    0xa100a2007300a1ull, 0x9100ab80a10091ull, 0x9000a100af0090ull, 0xaa00aa00aa00a1ull, 0xa9009c009700a3ull, 0xa100ab00a300a1ull, 0xa9009d009600a3ull, 0xa100ab00a300a1ull,
+    0xa900a1004200a1ull, 0xa90097009600a2ull, 0xa100a2007400a1ull, 0x9000ab80a10090ull, 0x9100ab80a10091ull, 0x9200ab00a10092ull, 0xaa00aa00aa00a1ull, 0xa900ab009e00a3ull,
+    0xa100ab00a300a1ull, 0xa900a1004300a1ull, 0xa900ab009800a2ull, 0xa100a2007500a1ull, 0x9200ab80a10092ull, 0x9000ab00a10090ull, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull,
+    0xa9009c009800a3ull, 0xa100ab00a300a1ull, 0xa9009e009600a3ull, 0xa100ab00a300a1ull, 0xa900a1004400a1ull, 0xa90098009600a2ull, 0xa100a2007600a1ull, 0x9000ab80a10090ull,
+    0x9200ab80a10092ull, 0x9100a100af0091ull, 0xaa00aa00aa00a1ull, 0xa900ab009e00a3ull, 0xa100ab00a300a1ull, 0xa900a1004500a1ull, 0xa900ab009800a2ull, 0xa100a2007700a1ull,
+    0x9200ab80a10092ull, 0x8f00ab00a1008full, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa900ab009b00a3ull, 0xa100ab00a300a1ull, 0xa900a1004600a1ull, 0xa900ab009500a2ull,
+    0xa100a2007800a1ull, 0x8f00ab80a1008full, 0x9000ab00a10090ull, 0xaa00aa00aa00a1ull, 0xa9009b009800a3ull, 0xa100ab00a300a1ull, 0xa9009e009500a3ull, 0xa100ab00a300a1ull,
+    0xa900a1004700a1ull, 0xa90098009500a2ull, 0xa100a2007900a1ull, 0x8f00ab80a1008full, 0x9200ab80a10092ull, 0x9100a100af0091ull, 0xaa00aa00aa00a1ull, 0xa9009e009900a3ull,
+    0xa100ab00a300a1ull, 0xa9009f009800a3ull, 0xa100ab00a300a1ull, 0xa900a1004800a1ull, 0xa90099009800a2ull, 0xa100a2007a00a1ull, 0x9300ab80a10093ull, 0x9200ab80a10092ull,
+    0x9400ab00a10094ull, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa9009c009a00a3ull, 0xa100ab00a300a1ull, 0xa900a0009600a3ull, 0xa100ab00a300a1ull, 0xa900a1004900a1ull,
+    0xa9009a009600a2ull, 0xa100a2007b00a1ull, 0x9400ab80a10094ull, 0x9000ab80a10090ull, 0x9300ab00a10093ull, 0x9100ab00a10091ull, 0xaa00aa00aa00a1ull, 0xa900ab00a000a3ull,
+    0xa100ab00a300a1ull, 0xa900a1004a00a1ull, 0xa900ab009a00a2ull, 0xa100a2007c00a1ull, 0x9400ab80a10094ull, 0x9300ab00a10093ull, 0x9000ab00a10090ull, 0xa900ab008f0083ull,
+    0x83007d00ac0083ull, 0xa900ab00900084ull, 0x84007e00ac0084ull, 0xa900ab00910085ull, 0x85007f00ac0085ull, 0xa900ab00920086ull, 0x86008000ac0086ull, 0xa900ab00930087ull,
+    0x87008100ac0087ull, 0xa900ab00940088ull, 0x88008200ac0088ull, 0xaa00aa00aa00a1ull, 0xa900ab002b00a3ull, 0xa100ab00a300a1ull, 0xa900a1007300a1ull, 0xaa00aa00aa00a2ull,
+    0xa100a2004100a1ull, 0x8500ab80a10085ull, 0x8400a100af0084ull, 0xaa00aa00aa00a1ull, 0xa9002a001f00a3ull, 0xa100ab00a300a1ull, 0xa9002b001e00a3ull, 0xa100ab00a300a1ull,
+    0xa900a1007400a1ull, 0xaa00aa00aa00a2ull, 0xa9006f002a00a3ull, 0xa200ab00a300a2ull, 0xa9006e002b00a3ull, 0xa200ab00a300a2ull, 0xa100a2004200a1ull, 0x8400ab80a10084ull,
+    0x8500ab80a10085ull, 0x8600ab00a10086ull, 0xaa00aa00aa00a1ull, 0xa900ab002c00a3ull, 0xa100ab00a300a1ull, 0xa900a1007500a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004300a1ull,
+    0x8600ab80a10086ull, 0x8400ab00a10084ull, 0x8500ab00a10085ull, 0xaa00aa00aa00a1ull, 0xa9002a002000a3ull, 0xa100ab00a300a1ull, 0xa9002c001e00a3ull, 0xa100ab00a300a1ull,
+    0xa900a1007600a1ull, 0xaa00aa00aa00a2ull, 0xa90070002a00a3ull, 0xa200ab00a300a2ull, 0xa9006e002c00a3ull, 0xa200ab00a300a2ull, 0xa100a2004400a1ull, 0x8400ab80a10084ull,
+    0x8600ab80a10086ull, 0x8500a100af0085ull, 0xaa00aa00aa00a1ull, 0xa900ab002c00a3ull, 0xa100ab00a300a1ull, 0xa900a1007700a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004500a1ull,
+    0x8600ab80a10086ull, 0x8300ab00a10083ull, 0x8500ab00a10085ull, 0xaa00aa00aa00a1ull, 0xa900ab002900a3ull, 0xa100ab00a300a1ull, 0xa900a1007800a1ull, 0xaa00aa00aa00a2ull,
+    0xa100a2004600a1ull, 0x8300ab80a10083ull, 0x8400ab00a10084ull, 0xaa00aa00aa00a1ull, 0xa90029002000a3ull, 0xa100ab00a300a1ull, 0xa9002c001d00a3ull, 0xa100ab00a300a1ull,
+    0xa900a1007900a1ull, 0xaa00aa00aa00a2ull, 0xa90070002900a3ull, 0xa200ab00a300a2ull, 0xa9006d002c00a3ull, 0xa200ab00a300a2ull, 0xa100a2004700a1ull, 0x8300ab80a10083ull,
+    0x8600ab80a10086ull, 0x8500a100af0085ull, 0xaa00aa00aa00a1ull, 0xa9002c002100a3ull, 0xa100ab00a300a1ull, 0xa9002d002000a3ull, 0xa100ab00a300a1ull, 0xa900a1007a00a1ull,
+    0xaa00aa00aa00a2ull, 0xa90071002c00a3ull, 0xa200ab00a300a2ull, 0xa90070002d00a3ull, 0xa200ab00a300a2ull, 0xa100a2004800a1ull, 0x8700ab80a10087ull, 0x8600ab80a10086ull,
+    0x8800ab00a10088ull, 0x8500ab00a10085ull, 0xaa00aa00aa00a1ull, 0xa9002a002200a3ull, 0xa100ab00a300a1ull, 0xa9002e001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007b00a1ull,
+    0xaa00aa00aa00a2ull, 0xa90072002a00a3ull, 0xa200ab00a300a2ull, 0xa9006e002e00a3ull, 0xa200ab00a300a2ull, 0xa100a2004900a1ull, 0x8800ab80a10088ull, 0x8400ab80a10084ull,
+    0x8700ab00a10087ull, 0x8500ab00a10085ull, 0xaa00aa00aa00a1ull, 0xa900ab002e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007c00a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004a00a1ull,
+    0x8800ab80a10088ull, 0x8700ab00a10087ull, 0x8400ab00a10084ull, 0x84008380020084ull, 0x85008380070085ull, 0x85008480080085ull, 0x860083800d0086ull, 0x860084800e0086ull,
+    0x860085800f0086ull, 0x87008480130087ull, 0x87008580140087ull, 0x87008680150087ull, 0x88008480180088ull, 0x88008580190088ull, 0x880086801a0088ull, 0x880087801b0088ull,
+    0xa9001c00880088ull, 0x87008880170087ull, 0xa9001600870087ull, 0x86008780110086ull, 0x86008880120086ull, 0xa9001000860086ull, 0x850086800a0085ull, 0x850087800b0085ull,
+    0x850088800c0085ull, 0xa9000900850085ull, 0x84008580040084ull, 0x84008680050084ull, 0x84008880060084ull, 0xa9000300840084ull, 0x83008680010083ull, 0xa9000000830083ull,
+    0xa900ab008f0089ull, 0x89007d00ad0089ull, 0x89008300ae0089ull, 0xa900ab0090008aull, 0x8a007e00ad008aull, 0x8a008400ae008aull, 0xa900ab0091008bull, 0x8b007f00ad008bull,
+    0x8b008500ae008bull, 0xa900ab0092008cull, 0x8c008000ad008cull, 0x8c008600ae008cull, 0xa900ab0093008dull, 0x8d008100ad008dull, 0x8d008700ae008dull, 0xa900ab0094008eull,
+    0x8e008200ad008eull, 0x8e008800ae008eull, 0xaa00aa00aa00a1ull, 0xa900ab003100a3ull, 0xa100ab00a300a1ull, 0xa900a1007300a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004100a1ull,
+    0x8b00ab80a1008bull, 0x8a00a100af008aull, 0xaa00aa00aa00a1ull, 0xa90030001f00a3ull, 0xa100ab00a300a1ull, 0xa90031001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007400a1ull,
+    0xaa00aa00aa00a2ull, 0xa9006f003000a3ull, 0xa200ab00a300a2ull, 0xa9006e003100a3ull, 0xa200ab00a300a2ull, 0xa100a2004200a1ull, 0x8a00ab80a1008aull, 0x8b00ab80a1008bull,
+    0x8c00ab00a1008cull, 0xaa00aa00aa00a1ull, 0xa900ab003200a3ull, 0xa100ab00a300a1ull, 0xa900a1007500a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004300a1ull, 0x8c00ab80a1008cull,
+    0x8a00ab00a1008aull, 0x8b00ab00a1008bull, 0xaa00aa00aa00a1ull, 0xa90030002000a3ull, 0xa100ab00a300a1ull, 0xa90032001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007600a1ull,
+    0xaa00aa00aa00a2ull, 0xa90070003000a3ull, 0xa200ab00a300a2ull, 0xa9006e003200a3ull, 0xa200ab00a300a2ull, 0xa100a2004400a1ull, 0x8a00ab80a1008aull, 0x8c00ab80a1008cull,
+    0x8b00a100af008bull, 0xaa00aa00aa00a1ull, 0xa900ab003200a3ull, 0xa100ab00a300a1ull, 0xa900a1007700a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004500a1ull, 0x8c00ab80a1008cull,
+    0x8900ab00a10089ull, 0x8b00ab00a1008bull, 0xaa00aa00aa00a1ull, 0xa900ab002f00a3ull, 0xa100ab00a300a1ull, 0xa900a1007800a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004600a1ull,
+    0x8900ab80a10089ull, 0x8a00ab00a1008aull, 0xaa00aa00aa00a1ull, 0xa9002f002000a3ull, 0xa100ab00a300a1ull, 0xa90032001d00a3ull, 0xa100ab00a300a1ull, 0xa900a1007900a1ull,
+    0xaa00aa00aa00a2ull, 0xa90070002f00a3ull, 0xa200ab00a300a2ull, 0xa9006d003200a3ull, 0xa200ab00a300a2ull, 0xa100a2004700a1ull, 0x8900ab80a10089ull, 0x8c00ab80a1008cull,
+    0x8b00a100af008bull, 0xaa00aa00aa00a1ull, 0xa90032002100a3ull, 0xa100ab00a300a1ull, 0xa90033002000a3ull, 0xa100ab00a300a1ull, 0xa900a1007a00a1ull, 0xaa00aa00aa00a2ull,
+    0xa90071003200a3ull, 0xa200ab00a300a2ull, 0xa90070003300a3ull, 0xa200ab00a300a2ull, 0xa100a2004800a1ull, 0x8d00ab80a1008dull, 0x8c00ab80a1008cull, 0x8e00ab00a1008eull,
+    0x8b00ab00a1008bull, 0xaa00aa00aa00a1ull, 0xa90030002200a3ull, 0xa100ab00a300a1ull, 0xa90034001e00a3ull, 0xa100ab00a300a1ull, 0xa900a1007b00a1ull, 0xaa00aa00aa00a2ull,
+    0xa90072003000a3ull, 0xa200ab00a300a2ull, 0xa9006e003400a3ull, 0xa200ab00a300a2ull, 0xa100a2004900a1ull, 0x8e00ab80a1008eull, 0x8a00ab80a1008aull, 0x8d00ab00a1008dull,
+    0x8b00ab00a1008bull, 0xaa00aa00aa00a1ull, 0xa900ab003400a3ull, 0xa100ab00a300a1ull, 0xa900a1007c00a1ull, 0xaa00aa00aa00a2ull, 0xa100a2004a00a1ull, 0x8e00ab80a1008eull,
+    0x8d00ab00a1008dull, 0x8a00ab00a1008aull, 0x8a00898002008aull, 0x8b00898007008bull, 0x8b008a8008008bull, 0x8c0089800d008cull, 0x8c008a800e008cull, 0x8c008b800f008cull,
+    0x8d008a8013008dull, 0x8d008b8014008dull, 0x8d008c8015008dull, 0x8e008a8018008eull, 0x8e008b8019008eull, 0x8e008c801a008eull, 0x8e008d801b008eull, 0xa9001c008e008eull,
+    0x8d008e8017008dull, 0xa90016008d008dull, 0x8c008d8011008cull, 0x8c008e8012008cull, 0xa90010008c008cull, 0x8b008c800a008bull, 0x8b008d800b008bull, 0x8b008e800c008bull,
+    0xa90009008b008bull, 0x8a008b8004008aull, 0x8a008c8005008aull, 0x8a008e8006008aull, 0xa90003008a008aull, 0x89008c80010089ull, 0xa9000000890089ull, 0x6d00ab007d006dull,
+    0x6d008300b0006dull, 0x6d008900b1006dull, 0x6e00ab007e006eull, 0x6e008400b0006eull, 0x6e008a00b1006eull, 0x6f00ab007f006full, 0x6f008500b0006full, 0x6f008b00b1006full,
+    0x7000ab00800070ull, 0x70008600b00070ull, 0x70008c00b10070ull, 0x7100ab00810071ull, 0x71008700b00071ull, 0x71008d00b10071ull, 0x7200ab00820072ull, 0x72008800b00072ull,
+    0x72008e00b10072ull,
+};
 }  // namespace coop
 
 
@@ -830,6 +927,31 @@ struct Mech {
       err = fmax(sqrt(err_sq / 7.0), 1.0e-10);
     }
     return __shfl_sync(0xffffffffu, err, 0);
+  }
+
+  // ---- tangent of one accepted step (forward sensitivities) ----
+  static constexpr int DYT = 109;     // dy in, dy_new out (NV)
+  static constexpr int DKR = 115;     // dk, the rate constants' tangent (NR)
+  static constexpr int TLM_CB = 169;  // constants of the tangent program
+  static constexpr int TLM_NCONST = 9;
+  static constexpr int NSLOTS_TLM = 178;
+  // dy_new = d(y_new)/d(y, k) (dy, dk) for one step of size h: walks
+  // coop::tlm_prog.  Requires attempt() for this step first (the LU of W and
+  // the K_i), y_n in S[Y..], dy in S[DYT..] and dk in S[DKR..].
+  template <class SA, class KA>
+  __device__ __forceinline__ static void tlm_step(SA& S, const KA& k, double h) {
+    for (int r = 0; r < NR; ++r) S[KT + r] = k(r);
+    for (int i = 0; i < TLM_NCONST; ++i) S[TLM_CB + i] = coop::tlm_const_val[i];
+    S[172] = -1.0156171083877703 / h;    // c21 / h
+    S[173] = 4.0759956452537702 / h;    // c31 / h
+    S[174] = 9.20767942983308 / h;    // c32 / h
+    for (int n = 0; n < coop::TLM_OPS; ++n) {
+      const unsigned long long w = __ldg(coop::tlm_prog + n);
+      const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+      const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^
+                                            ((long long)(lo >> 31) << 63));
+      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);
+    }
   }
 
   // ---- discrete adjoint of one accepted step ----

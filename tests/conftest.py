@@ -21,7 +21,20 @@ def _cuda_available() -> bool:
         return False
 
 
+# GPU test modules in the order they run (under -x a failure stops the rest):
+# those that have passed on a GB300 first, the newer ones after them, and the
+# allocation-free entry point last.  Other modules keep their place before them.
+GPU_ORDER = ("test_gpu_adjoint", "test_gpu_parity", "test_gpu_scale", "test_gpu_ts1", "test_gpu_tuning",
+             "test_gpu_tangent", "test_zz_no_alloc")
+
+
+def _gpu_rank(item):
+    name = item.module.__name__.rsplit(".", 1)[-1] if item.module else ""
+    return GPU_ORDER.index(name) + 1 if name in GPU_ORDER else 0
+
+
 def pytest_collection_modifyitems(config, items):
+    items.sort(key=_gpu_rank)
     if _cuda_available():
         return
     skip = pytest.mark.skip(reason="no CUDA device")

@@ -54,4 +54,22 @@ void hostsim_adjoint(double* slots, const double* k, double h, int* status) {
   *status = st;
 }
 
+// DYT, DKR, NSLOTS_TLM
+int hostsim_tlm_layout(int* out) {
+  out[0] = Mech::DYT;
+  out[1] = Mech::DKR;
+  out[2] = Mech::NSLOTS_TLM;
+  return 0;
+}
+
+// The tangent of one step of size h: attempt(), then tlm_step() (dy in
+// S[DYT..] and dk in S[DKR..] in, dy_new in S[DYT..] out).
+void hostsim_tlm(double* slots, const double* k, double h, int* status) {
+  Store S{slots};
+  int st = 0;
+  Mech::attempt(S, Rates{k}, h, st);
+  Mech::tlm_step(S, Rates{k}, h);
+  *status = st;
+}
+
 }  // extern "C"
