@@ -23,7 +23,10 @@ LIB = PKG / "lib"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99", "ts1")
+# Libraries build() makes by default.  saprcnov (96 species, as large as
+# SAPRC99 to compile, no benchmark configuration) is built on request:
+# build(("saprcnov",)).
+DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99", "ts1", "saprc99_mini")
 
 
 def nvcc() -> str:

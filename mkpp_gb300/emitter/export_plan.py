@@ -95,6 +95,42 @@ def _rename(text: str) -> str:
     return text.replace("ENV_T", "T").replace("ENV_RHO", "RHO")
 
 
+def _env_names(text: str, runtime_env: bool, env_t: float, env_rho: float) -> str:
+    """Temperature and air-density names left in a printed rate constant.
+
+    The lowering keeps some rate laws as one opaque symbol whose name is the
+    legacy C text (e.g. ``2.45e-12*exp(-1775.0e0/TEMP)``); the reference's
+    printer resolves the names inside it (src/mkpp/format_eqn.py:136-164):
+    TEMP, temp and Temp are the temperature and M_density the air density,
+    per cell with a runtime environment, else the compile-time values."""
+    t = "T" if runtime_env else repr(env_t)
+    rho = "RHO" if runtime_env else repr(env_rho)
+    text = re.sub(r"\b(?:TEMP|temp|Temp)\b", t, text)
+    return re.sub(r"\bM_density\b", rho, text)
+
+
+# Legacy species the reference's printer sets to 1 in every printed
+# expression (src/mkpp/format_eqn.py:136-146).
+UNIT_SPECIES = ("DummyCH4", "DummyNMVOC", "FixedOH", "FixedCl")
+
+
+def _check_mass_action(mech) -> None:
+    """Refuse mechanisms whose reference tendencies are not k * monomial sums.
+
+    * Equilibrium coupling adds a relaxation flux towards an analytical
+      partition model to F (src/mkpp/lowering.py:375-410).
+    * A unit species that is a variable species and a reactant: the printer
+      substitutes 1 for it after the symbolic Jacobian is taken, so the
+      reference's J keeps a column for it that F no longer depends on."""
+    if getattr(mech, "equilibrium_reactions", None):
+        raise NotImplementedError(f"{mech.name}: equilibrium coupling is not a mass-action tendency")
+    for r in mech.reactions:
+        names = r.reactants if isinstance(r.reactants, dict) else {x: 1.0 for x in r.reactants}
+        unit = [n for n in names if n in UNIT_SPECIES and any(s.name == n and s.role != "fixed" for s in mech.species)]
+        if unit:
+            raise NotImplementedError(f"{mech.name}: reactant {unit[0]} is printed as 1 after differentiation")
+
+
 def export(mkpp_src: str, mechanism: str, rtol: float | None, atol: float | None,
            solver: str = "ros3", seed: float | None = None,
            temperature: float = 298.15, air_density: float = 2.46e19) -> dict:
@@ -113,6 +149,7 @@ def export(mkpp_src: str, mechanism: str, rtol: float | None, atol: float | None
     from mkpp.template_context import build_template_context
 
     mech = load_mechanism(mechanism)
+    _check_mass_action(mech)
     if not getattr(mech, "metadata", None):
         mech.metadata = {}
     # Same metadata wiring as run_compiler (src/mkpp/cli.py:223-236).
@@ -146,8 +183,8 @@ def export(mkpp_src: str, mechanism: str, rtol: float | None, atol: float | None
         sp.Symbol("S_a", real=True, nonnegative=True): sp.Float(1.0),
         sp.Symbol("v_gas", real=True, nonnegative=True): sp.Float(1.0),
     }
-    for dummy in ("C_DummyCH4", "C_DummyNMVOC", "C_FixedOH", "C_FixedCl"):
-        subs[sp.Symbol(dummy)] = sp.Float(1.0)
+    for name in UNIT_SPECIES:
+        subs[sp.Symbol(f"C_{name}")] = sp.Float(1.0)
     temp_sym = sp.Symbol("Temp", real=True, nonnegative=True)
     rho_sym = sp.Symbol("M_density", real=True, nonnegative=True)
     env_T = sp.Symbol("ENV_T", real=True)
@@ -186,7 +223,12 @@ def export(mkpp_src: str, mechanism: str, rtol: float | None, atol: float | None
             if name in var_index:
                 net[species.index(name)] = net.get(species.index(name), 0.0) + float(y)
         net_list = [[s, c] for s, c in net.items() if c != 0.0]
-        text = _rename(_c_expr(k_expr, sp))
+        if flux == 0:
+            # A rate constant that is identically zero (an Arrhenius A of 0.0)
+            # makes the lowered flux 0: the reaction enters neither F nor the
+            # Jacobian's sparsity pattern (src/mkpp/lowering.py:167-432).
+            var_reactants, net_list = [], []
+        text = _env_names(_rename(_c_expr(k_expr, sp)), runtime_env, env_t, env_rho)
         if re.search(r"\bC_\w+", text):
             raise ValueError(f"reaction {r_idx}: unmapped species symbol in rate constant: {text}")
         # Derivatives of the rate constant with respect to fixed species, for

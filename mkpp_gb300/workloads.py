@@ -23,6 +23,14 @@ Workloads (cells, host steps x dt):
   maxima Jmax_r log-uniform in [1e-6, 1e-2] 1/s (NO2 -> 8e-3 1/s).
 * ``ts1``           1048576 cells, 6 x 600 s, mol/m3 units (molec/cm3 / 6.02214076e17),
   40 % night, 30 % clean (NOx x 0.01), 30 % polluted (NOx x 100).
+
+Further mechanisms the reference ships (no benchmark configuration; parity
+cases only):
+
+* ``saprc99_mini``, ``saprcnov``  65536 cells, 24 x 600 s, drawn as
+  ``saprc99`` (background species AIR, M, O2, N2, H2O, CH4, H2, CO2 set from
+  p, T and RH where the mechanism has them; saprcnov's fixed RO2 log-uniform
+  in [1e6, 1e9]); the NO2 photolysis slot at 8e-3 1/s.
 """
 
 from __future__ import annotations
@@ -191,7 +199,61 @@ def ts1(ncells: int = 1048576, seed: int = SEED) -> Workload:
     return w
 
 
-BUILDERS = {"chapman": chapman, "small_strato": small_strato, "saprc99": saprc99, "ts1": ts1}
+def _photolysis_slot(raw, species):
+    """Runtime parameter slot of the photolysis whose only reactant is `species`."""
+    ix = _species_index(raw)[species]
+    for ph in raw["photolysis_reactions"]:
+        r = raw["reactions"][ph["reaction_idx"]]
+        if [s for s, _ in r["reactants"]] == [ix]:
+            return ph["photo_idx"]
+    return None
+
+
+def _background(raw, conc, M, T, rh):
+    """Air, its major components and the long-lived background species."""
+    ix = _species_index(raw)
+    es = 610.94 * np.exp(17.625 * (T - 273.15) / (T - 30.11))     # Magnus, Pa
+    fixed = {"AIR": M, "M": M, "O2": 0.21 * M, "N2": 0.78 * M, "H2O": rh * es / (K_B * T) * 1e-6,
+             "CH4": 1.8e-6 * M, "H2": 5.5e-7 * M, "CO2": 4.2e-4 * M}
+    for name, v in fixed.items():
+        if name in ix:
+            conc[ix[name]] = v
+
+
+def _saprc_family(name: str, ncells: int, seed: int) -> Workload:
+    raw = load_raw(name)
+    rng = np.random.default_rng(seed)
+    ix = _species_index(raw)
+    T = rng.uniform(250.0, 315.0, ncells)
+    p = rng.uniform(5e4, 1.05e5, ncells)
+    M = p / (K_B * T) * 1e-6
+    rh = rng.uniform(0.1, 0.9, ncells)
+    conc = _loguniform(rng, 1e-2, 1e12, (len(raw["species"]), ncells))
+    factor = _loguniform(rng, 0.01, 100.0, ncells)
+    for s in ("NO", "NO2", *VOC_SAPRC99):
+        if s in ix:
+            conc[ix[s]] *= factor
+    _background(raw, conc, M, T, rh)
+    if "RO2" in ix and raw["fixed"][ix["RO2"]]:
+        conc[ix["RO2"]] = _loguniform(rng, 1e6, 1e9, ncells)
+    phase = rng.uniform(0.0, 2.0 * np.pi, ncells)
+    jmax = _jmax(raw, rng, no2_slot=_photolysis_slot(raw, "NO2"))
+    param = np.zeros((raw["num_rate_parameters"], ncells))
+    w = Workload(name, name, conc, T, p, M.copy(), rh, param, 600.0, 24, phase=phase, jmax=jmax)
+    w.param = w.param_at(0)
+    return w
+
+
+def saprc99_mini(ncells: int = 65536, seed: int = SEED) -> Workload:
+    return _saprc_family("saprc99_mini", ncells, seed)
+
+
+def saprcnov(ncells: int = 65536, seed: int = SEED) -> Workload:
+    return _saprc_family("saprcnov", ncells, seed)
+
+
+BUILDERS = {"chapman": chapman, "small_strato": small_strato, "saprc99": saprc99, "ts1": ts1,
+            "saprc99_mini": saprc99_mini, "saprcnov": saprcnov}
 
 
 def make(name: str, ncells: int | None = None, seed: int = SEED) -> Workload:

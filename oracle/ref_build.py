@@ -35,6 +35,8 @@ HERE = Path(__file__).resolve().parent
 REF = HERE / "_ref"
 GEN = REF / "gen"
 MECHS = ("chapman", "small_strato", "saprc99")
+# Further shipped mechanisms, built on demand by the parity tests (ensure()).
+EXTRA_MECHS = ("saprc99_mini", "saprcnov")
 DEFAULT_REFERENCE = "/root/reference"
 
 
@@ -135,6 +137,17 @@ def compile_shipped(mech: str, reference: str = DEFAULT_REFERENCE) -> Path | Non
     return out
 
 
+def ensure(mech: str, reference: str = DEFAULT_REFERENCE):
+    """RefSolver for mech, regenerated and compiled first where the reference
+    checkout (or headers generated from it earlier) is present; else None."""
+    if Path(reference).exists():
+        generate(mech, reference)
+    if not (GEN / mech / f"{mech}.hpp").exists():
+        return None
+    compile_driver(mech)
+    return RefSolver(mech)
+
+
 def build_if_available(reference: str = DEFAULT_REFERENCE) -> list[Path]:
     built = []
     for mech in MECHS:
@@ -164,27 +177,28 @@ class RefSolver:
         conc = np.ascontiguousarray(conc, dtype=np.float64)
         n = conc.shape[1]
         full = lambda a, v: np.ascontiguousarray(np.full(n, v) if a is None else a, dtype=np.float64)  # noqa: E731
-        T, RHO, RH = full(temp, 298.15), full(rho, 2.46e19), full(rh, 0.5)
+        T, RHO, RH, CLW = full(temp, 298.15), full(rho, 2.46e19), full(rh, 0.5), full(clw, 0.0)
         P = np.zeros((max(1, self.np_), n)) if param is None else np.ascontiguousarray(param, dtype=np.float64)
         vp = C.c_void_p
         rc = self.lib.mkpp_ref_integrate(C.c_int(n), vp(conc.ctypes.data), vp(T.ctypes.data), vp(RH.ctypes.data),
-                                         vp(RHO.ctypes.data), vp(P.ctypes.data), C.c_int(P.shape[0]),
+                                         vp(CLW.ctypes.data), vp(RHO.ctypes.data), vp(P.ctypes.data),
+                                         C.c_int(P.shape[0]),
                                          C.c_double(dt), C.c_int(steps), C.c_int(nthreads),
                                          C.c_double(-1.0 if seed is None else seed))
         return {"conc": conc, "status": np.zeros(n, np.int32), "rc": rc}
 
-    def evaluate(self, conc, temp=None, rho=None, rh=None, param=None, **_):
+    def evaluate(self, conc, temp=None, rho=None, rh=None, param=None, clw=None, **_):
         """(F [ns][cells], J [ns][ns][cells]) from compute_rates / compute_jacobian."""
         conc = np.ascontiguousarray(conc, dtype=np.float64)
         n = conc.shape[1]
         full = lambda a, v: np.ascontiguousarray(np.full(n, v) if a is None else a, dtype=np.float64)  # noqa: E731
-        T, RHO, RH = full(temp, 298.15), full(rho, 2.46e19), full(rh, 0.5)
+        T, RHO, RH, CLW = full(temp, 298.15), full(rho, 2.46e19), full(rh, 0.5), full(clw, 0.0)
         P = np.zeros((max(1, self.np_), n)) if param is None else np.ascontiguousarray(param, dtype=np.float64)
         F = np.zeros((self.ns, n))
         J = np.zeros((self.ns, self.ns, n))
         vp = C.c_void_p
-        args = (C.c_int(n), vp(conc.ctypes.data), vp(T.ctypes.data), vp(RH.ctypes.data), vp(RHO.ctypes.data),
-                vp(P.ctypes.data), C.c_int(P.shape[0]))
+        args = (C.c_int(n), vp(conc.ctypes.data), vp(T.ctypes.data), vp(RH.ctypes.data), vp(CLW.ctypes.data),
+                vp(RHO.ctypes.data), vp(P.ctypes.data), C.c_int(P.shape[0]))
         self.lib.mkpp_ref_rates(*args, vp(F.ctypes.data))
         self.lib.mkpp_ref_jacobian(*args, vp(J.ctypes.data))
         return F, J

@@ -27,10 +27,11 @@ using StateView = Kokkos::View<double*, Kokkos::LayoutStride, Kokkos::HostSpace>
 // gating add trailing arguments).  A template so that only the matching
 // branch is instantiated.
 template <class S>
-void step(const S& solver, double dt, StateView& state, const ParamView& jvals, double t, double rh, double rho) {
+void step(const S& solver, double dt, StateView& state, const ParamView& jvals, double t, double rh, double clw,
+          double rho) {
   if constexpr (S::SUPPORTS_RUNTIME_ENVIRONMENT) {
     if constexpr (S::HAS_CLOUD_GATED) {
-      solver.integrate(dt, state, jvals, t, rh, 0.0, rho);
+      solver.integrate(dt, state, jvals, t, rh, clw, rho);
     } else {
       solver.integrate(dt, state, jvals, t, rh, rho);
     }
@@ -40,18 +41,28 @@ void step(const S& solver, double dt, StateView& state, const ParamView& jvals, 
 }
 
 template <class S, class V, class O>
-void rates(const S& solver, const V& state, O& out, const ParamView& jvals, double t, double rh, double rho) {
+void rates(const S& solver, const V& state, O& out, const ParamView& jvals, double t, double rh, double clw,
+           double rho) {
   if constexpr (S::SUPPORTS_RUNTIME_ENVIRONMENT) {
-    solver.compute_rates(state, out, jvals, t, rh, rho);
+    if constexpr (S::HAS_CLOUD_GATED) {
+      solver.compute_rates(state, out, jvals, t, rh, clw, rho);
+    } else {
+      solver.compute_rates(state, out, jvals, t, rh, rho);
+    }
   } else {
     solver.compute_rates(state, out, jvals);
   }
 }
 
 template <class S, class V, class O>
-void jacobian(const S& solver, const V& state, O& out, const ParamView& jvals, double t, double rh, double rho) {
+void jacobian(const S& solver, const V& state, O& out, const ParamView& jvals, double t, double rh, double clw,
+              double rho) {
   if constexpr (S::SUPPORTS_RUNTIME_ENVIRONMENT) {
-    solver.compute_jacobian(state, out, jvals, t, rh, rho);
+    if constexpr (S::HAS_CLOUD_GATED) {
+      solver.compute_jacobian(state, out, jvals, t, rh, clw, rho);
+    } else {
+      solver.compute_jacobian(state, out, jvals, t, rh, rho);
+    }
   } else {
     solver.compute_jacobian(state, out, jvals);
   }
@@ -63,9 +74,11 @@ extern "C" {
 int mkpp_ref_num_species() { return Solver::NUM_SPECIES; }
 int mkpp_ref_num_parameters() { return Solver::NUM_RUNTIME_PARAMETERS; }
 
-// conc[s * ncells + c] (in/out), param[p * ncells + c] with nparam rows.
-int mkpp_ref_integrate(int ncells, double* conc, const double* temp, const double* rh, const double* rho,
-                       const double* param, int nparam, double dt, int steps, int nthreads, double seed) {
+// conc[s * ncells + c] (in/out), param[p * ncells + c] with nparam rows; clw
+// (cloud liquid water, cloud-gated mechanisms only) may be null for 0.
+int mkpp_ref_integrate(int ncells, double* conc, const double* temp, const double* rh, const double* clw,
+                       const double* rho, const double* param, int nparam, double dt, int steps, int nthreads,
+                       double seed) {
   if (nthreads > 0) omp_set_num_threads(nthreads);
   const int np = Solver::NUM_RUNTIME_PARAMETERS > 0 ? Solver::NUM_RUNTIME_PARAMETERS : 1;
 #pragma omp parallel
@@ -78,15 +91,16 @@ int mkpp_ref_integrate(int ncells, double* conc, const double* temp, const doubl
       for (int p = 0; p < np; ++p) forcing[p] = p < nparam ? param[(size_t)p * ncells + c] : 0.0;
       ParamView jvals(forcing.data(), (std::size_t)np);
       StateView state(conc + c, Solver::NUM_SPECIES, (std::size_t)ncells);
-      for (int s = 0; s < steps; ++s) step(solver, dt, state, jvals, temp[c], rh[c], rho[c]);
+      const double w = clw ? clw[c] : 0.0;
+      for (int s = 0; s < steps; ++s) step(solver, dt, state, jvals, temp[c], rh[c], w, rho[c]);
     }
   }
   return 0;
 }
 
 // Tendencies F[s * ncells + c] from the reference's compute_rates().
-int mkpp_ref_rates(int ncells, const double* conc, const double* temp, const double* rh, const double* rho,
-                   const double* param, int nparam, double* out) {
+int mkpp_ref_rates(int ncells, const double* conc, const double* temp, const double* rh, const double* clw,
+                   const double* rho, const double* param, int nparam, double* out) {
   const int np = Solver::NUM_RUNTIME_PARAMETERS > 0 ? Solver::NUM_RUNTIME_PARAMETERS : 1;
   std::vector<double> forcing(np, 0.0);
   Solver solver;
@@ -97,14 +111,14 @@ int mkpp_ref_rates(int ncells, const double* conc, const double* temp, const dou
                                                                                (std::size_t)ncells);
     StateView f(out + c, Solver::NUM_SPECIES, (std::size_t)ncells);
     for (int s = 0; s < Solver::NUM_SPECIES; ++s) f(s) = 0.0;
-    rates(solver, state, f, jvals, temp[c], rh[c], rho[c]);
+    rates(solver, state, f, jvals, temp[c], rh[c], clw ? clw[c] : 0.0, rho[c]);
   }
   return 0;
 }
 
 // Dense Jacobian J[(i * NS + j) * ncells + c] = dF_i/dC_j from compute_jacobian().
-int mkpp_ref_jacobian(int ncells, const double* conc, const double* temp, const double* rh, const double* rho,
-                      const double* param, int nparam, double* out) {
+int mkpp_ref_jacobian(int ncells, const double* conc, const double* temp, const double* rh, const double* clw,
+                      const double* rho, const double* param, int nparam, double* out) {
   const int np = Solver::NUM_RUNTIME_PARAMETERS > 0 ? Solver::NUM_RUNTIME_PARAMETERS : 1;
   const std::size_t ns = Solver::NUM_SPECIES;
   std::vector<double> forcing(np, 0.0);
@@ -116,7 +130,7 @@ int mkpp_ref_jacobian(int ncells, const double* conc, const double* temp, const 
     Kokkos::View<const double*, Kokkos::LayoutStride, Kokkos::HostSpace> state(conc + c, ns, (std::size_t)ncells);
     Kokkos::View<double**, Kokkos::LayoutStride, Kokkos::HostSpace> jac(out + c, ns, ns, ns * ncells,
                                                                          (std::size_t)ncells);
-    jacobian(solver, state, jac, jvals, temp[c], rh[c], rho[c]);
+    jacobian(solver, state, jac, jvals, temp[c], rh[c], clw ? clw[c] : 0.0, rho[c]);
   }
   return 0;
 }

@@ -25,7 +25,7 @@ small JSON fixtures, so the tests never need the reference at run time:
   regenerated and compiled by oracle/ref_build.py) at the inputs above,
   with the photolysis slots scaled by 1.0 and by 1.05.
 
-Usage: python tests/golden/make_golden.py --reference <MKPP checkout>
+Usage: python tests/golden/make_golden.py --reference <MKPP checkout> [--lu-only]
 """
 import argparse
 import hashlib
@@ -34,6 +34,9 @@ import re
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+# Mechanisms whose shipped LU tables are pinned; the large ones as a digest.
+LU_MECHS = ("chapman", "small_strato", "saprc99", "ts1", "saprc99_mini", "saprcnov")
+LU_DIGEST = ("ts1", "saprcnov")
 
 
 def tables(text: str, name: str):
@@ -45,10 +48,33 @@ def tables(text: str, name: str):
     return [int(x) for x in body.replace(" ", "").replace("\n", "").split(",") if x]
 
 
+def lu_tables(ref: Path):
+    for mech in LU_MECHS:
+        fac = (ref / f"mkpp-generated/{mech}/supernodal_factorize.hpp").read_text()
+        sol = (ref / f"mkpp-generated/{mech}/supernodal_solve.hpp").read_text()
+        out = {
+            "source": f"mkpp-generated/{mech}/supernodal_factorize.hpp, supernodal_solve.hpp",
+            "operations": tables(fac, "operations"), "products": tables(fac, "products"),
+            "lower_offsets": tables(sol, "lower_offsets"), "upper_offsets": tables(sol, "upper_offsets"),
+            "diagonal": tables(sol, "diagonal"), "lower": tables(sol, "lower"), "upper": tables(sol, "upper"),
+        }
+        if mech in LU_DIGEST:
+            # Large: keep counts and a digest of the canonical tables only.
+            canon = json.dumps({k: v for k, v in out.items() if k != "source"}, separators=(",", ":"), sort_keys=True)
+            out = {"source": out["source"], "n_operations": len(out["operations"]), "n_products": len(out["products"]),
+                   "sha256": hashlib.sha256(canon.encode()).hexdigest()}
+        (HERE / f"lu_tables_{mech}.json").write_text(json.dumps(out, separators=(",", ":")))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
-    ref = Path(ap.parse_args().reference)
+    ap.add_argument("--lu-only", action="store_true", help="write the lu_tables_<mech>.json fixtures only")
+    args = ap.parse_args()
+    ref = Path(args.reference)
+    lu_tables(ref)
+    if args.lu_only:
+        return
     run = json.loads((ref / "reports/native-kokkos-5.1.1/final-mkpp-chapman.stdout.json").read_text())
     vals = run["state"]["checkpoints"][0]["values"]
     (HERE / "chapman_kokkos_10x60.json").write_text(json.dumps({
@@ -63,21 +89,6 @@ def main():
     keep["source"] = "tests/integration/e2e_validation/data/chapman_reference.json"
     keep["gate"] = {"rtol": 1e-4, "atol": 1.0, "source": "tests/integration/e2e_validation/test_scipy_validation.cpp:246-247"}
     (HERE / "chapman_scipy_reference.json").write_text(json.dumps(keep, indent=1))
-    for mech in ("chapman", "small_strato", "saprc99", "ts1"):
-        fac = (ref / f"mkpp-generated/{mech}/supernodal_factorize.hpp").read_text()
-        sol = (ref / f"mkpp-generated/{mech}/supernodal_solve.hpp").read_text()
-        out = {
-            "source": f"mkpp-generated/{mech}/supernodal_factorize.hpp, supernodal_solve.hpp",
-            "operations": tables(fac, "operations"), "products": tables(fac, "products"),
-            "lower_offsets": tables(sol, "lower_offsets"), "upper_offsets": tables(sol, "upper_offsets"),
-            "diagonal": tables(sol, "diagonal"), "lower": tables(sol, "lower"), "upper": tables(sol, "upper"),
-        }
-        if mech == "ts1":
-            # Large: keep counts and a digest of the canonical tables only.
-            canon = json.dumps({k: v for k, v in out.items() if k != "source"}, separators=(",", ":"), sort_keys=True)
-            out = {"source": out["source"], "n_operations": len(out["operations"]), "n_products": len(out["products"]),
-                   "sha256": hashlib.sha256(canon.encode()).hexdigest()}
-        (HERE / f"lu_tables_{mech}.json").write_text(json.dumps(out, separators=(",", ":")))
     kat = (ref / "tests/integration/supernodal_factorization/test_factorization_parity.cpp").read_text()
     w = [float(x) for x in re.search(r"COMPACT_SIZE> w\{(.*?)\};", kat, re.S).group(1).replace("\n", "").split(",")]
     dense = [float(x) for x in re.search(r"dense_logical_matrix\{(.*?)\};", kat, re.S).group(1).replace("\n", "").split(",")]

@@ -14,7 +14,8 @@ the GPU build (--fmad=false).  For one attempt on seeded cells:
   small_strato 1e-12 at cond 1e5, SAPRC99 2.5e-10 at cond 3e8).  So the
   step size per mechanism keeps cond(W) below ~1e9 on these cells.
 SAPRC99 runs with its three 1e33-1e37 1/s rate constants moderated to 1e3,
-as in the GPU forced-step test.
+as in the GPU forced-step test, and so do saprc99_mini and saprcnov (the
+same Troe rates), which get the first two checks too.
 """
 
 import ctypes as C
@@ -31,18 +32,33 @@ from mkpp_gb300.emitter.plan import load
 from oracle.oracle import Oracle
 
 MECHS = ["chapman", "small_strato", "saprc99"]
+# Further mechanisms the reference ships, checked for the forward step.
+EXTRA = ["saprc99_mini", "saprcnov"]
 # Step sizes of the oracle comparison: cond(W) at most ~10, 1.5e5, 3e8 and
 # (TS1, where a 1 s step already changes the state by O(1)) 2e10.
-H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6, "ts1": 1.0}
+H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6, "ts1": 1.0, "saprc99_mini": 1e-6,
+            "saprcnov": 1e-6}
 # Rate constants of the shipped mechanisms that reach 1e29-1e41 1/s (Troe k0
 # evaluated as A exp(+C/T)); moderated to 1e3 as in the GPU forced-step test.
-EXTREME = {"saprc99": (11, 32, 69), "ts1": (375, 376, 383, 394, 397, 402)}
+EXTREME = {"saprc99": (11, 32, 69), "ts1": (375, 376, 383, 394, 397, 402), "saprc99_mini": (7,),
+           "saprcnov": (10, 31, 57)}
+
+
+class _Libs(dict):
+    """Hostsim libraries by mechanism, each compiled on first use."""
+
+    def __init__(self, out):
+        super().__init__()
+        self.out = out
+
+    def __missing__(self, mech):
+        self[mech] = hostsim_lib.compile(self.out, mech)
+        return self[mech]
 
 
 @pytest.fixture(scope="module")
 def hostsim(tmp_path_factory):
-    out = tmp_path_factory.mktemp("hostsim")
-    return {m: hostsim_lib.compile(out, m) for m in MECHS}
+    return _Libs(tmp_path_factory.mktemp("hostsim"))
 
 
 _layout = hostsim_lib.layout
@@ -72,7 +88,7 @@ def _case(mech, n=4):
     return w, o, k, dk
 
 
-@pytest.mark.parametrize("mech", MECHS)
+@pytest.mark.parametrize("mech", MECHS + EXTRA)
 def test_per_thread_attempt_equals_cooperative_programs(hostsim, mech):
     lib = hostsim[mech]
     L = _layout(lib)
@@ -106,13 +122,13 @@ def test_per_thread_attempt_equals_cooperative_programs(hostsim, mech):
         assert np.array_equal(S[:nlu], P[:nlu])
 
 
-@pytest.mark.parametrize("mech", MECHS)
+@pytest.mark.parametrize("mech", MECHS + EXTRA)
 def test_per_thread_step_matches_oracle_with_forced_step(hostsim, mech):
     _forced_step_vs_oracle(hostsim[mech], mech)
 
 
-def test_ts1_table_step_matches_oracle_with_forced_step(tmp_path):
-    _forced_step_vs_oracle(_compile(tmp_path, "ts1"), "ts1")
+def test_ts1_table_step_matches_oracle_with_forced_step(hostsim):
+    _forced_step_vs_oracle(hostsim["ts1"], "ts1")
 
 
 def _forced_step_vs_oracle(lib, mech):
@@ -169,12 +185,12 @@ def test_table_attempt_equals_unrolled_attempt(hostsim, mech, tmp_path):
             assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
 
 
-def test_ts1_table_attempt_equals_its_programs(tmp_path):
+def test_ts1_table_attempt_equals_its_programs(hostsim):
     """TS1 (210 species, 49299 LU multiply-adds) is emitted table-driven: its
     host-compiled per-thread attempt gives the stage vectors and LU of its
     stage programs executed in program order with exactly rounded fma."""
     mech = "ts1"
-    lib = _compile(tmp_path, mech)
+    lib = hostsim[mech]
     L = _layout(lib)
     plan = load(mech)
     cuda_emitter.emit_mechanism(plan)
@@ -243,13 +259,13 @@ def test_table_adjoint_equals_unrolled_adjoint(hostsim, mech, tmp_path):
             assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2] == 0
 
 
-def test_ts1_table_adjoint_matches_dense_adjoint(tmp_path):
+def test_ts1_table_adjoint_matches_dense_adjoint(hostsim):
     """TS1's table-driven adjoint of one step against the dense FP64 CPU
     adjoint (oracle/adjoint_ref.py), scale-free: |dg * x| <= 1e-8 max|g * x|
     for x = y_n and x = k (measured: 1e-17 and 1e-11)."""
     from oracle.adjoint_ref import DenseModel
 
-    lib = _compile(tmp_path, "ts1")
+    lib = hostsim["ts1"]
     plan = load("ts1")
     dm = DenseModel("ts1")
     w, o, k, _ = _case("ts1", 2)
@@ -268,10 +284,6 @@ def test_ts1_table_adjoint_matches_dense_adjoint(tmp_path):
 
 
 _host_tlm = hostsim_lib.tangent_step
-
-
-def _tlm_lib(hostsim, mech, tmp_path):
-    return hostsim[mech] if mech in hostsim else _compile(tmp_path, mech)
 
 
 def _jacobians(lib, mech, y, k, h):
@@ -302,8 +314,8 @@ def _column_error(a, b):
     return (np.abs(a - b).max(axis=0) / scale).max()
 
 
-@pytest.mark.parametrize("mech", MECHS + ["ts1"])
-def test_tangent_is_the_transpose_of_the_adjoint(hostsim, mech, tmp_path):
+@pytest.mark.parametrize("mech", MECHS + EXTRA + ["ts1"])
+def test_tangent_is_the_transpose_of_the_adjoint(hostsim, mech):
     """For one step, the emitted tangent (tlm_step) and adjoint
     (adjoint_step) give the same derivative: every column of d y_new/d y and
     d y_new/d k from the tangent equals the adjoint's to 64 eps cond(W) of
@@ -315,7 +327,7 @@ def test_tangent_is_the_transpose_of_the_adjoint(hostsim, mech, tmp_path):
     tests check the same transpose identity, test_adjoint_identity.py.)"""
     from oracle.adjoint_ref import DenseModel
 
-    lib = _tlm_lib(hostsim, mech, tmp_path)
+    lib = hostsim[mech]
     plan = load(mech)
     dm = DenseModel(mech)
     w, o, k, _ = _case(mech, 1)

@@ -1,0 +1,91 @@
+"""Further shipped mechanisms on the GPU: saprc99_mini (17 species, 13 reactions).
+
+The same kernels and checks as the SAPRC99 parity tests, on a mechanism the
+reference ships without a benchmark configuration:
+* rate constants against the oracle, 1e-13 relative;
+* forced step sequence (the oracle replays the GPU's attempted step sizes and
+  accept flags): per species 1e-9 (|oracle| + atol), with the one shipped
+  Troe rate of ~1e33 1/s (reaction 7) moderated to 1e3 as for SAPRC99;
+* cells parked for the warp-cooperative kernel end bit-identical to cells
+  that stay on one lane.
+On the CPU the oracle matches the reference's own generated solver for this
+mechanism (tests/test_oracle_reference.py) and the emitted code matches the
+oracle's forced step (tests/test_emitted_host.py).
+"""
+import numpy as np
+import pytest
+
+from mkpp_gb300 import workloads
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+MECH = "saprc99_mini"
+EXTREME = (7,)
+CELLS = 256
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mkpp_gb300 import build
+
+    return build.build((MECH,))[0]
+
+
+def _setup():
+    import torch
+
+    from mkpp_gb300.api import DeviceSolver
+
+    w = workloads.make(MECH, CELLS)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    return w, DeviceSolver(MECH), Oracle(MECH), d
+
+
+def test_rate_constants(lib):
+    w, s, o, d = _setup()
+    k_gpu, status = s.rate_constants(d(w.conc), d(w.temp), d(w.rho), d(w.rh), None, d(w.param))
+    k_ref, _ = o.rate_constants(w.conc, w.temp, w.rho, w.rh, None, w.param)
+    np.testing.assert_allclose(k_gpu.cpu().numpy(), k_ref, rtol=1e-13, atol=0)
+    assert int(status.sum()) == 0
+
+
+def test_forced_step_sequence_parity(lib):
+    import torch
+
+    w, s, o, d = _setup()
+    conc = d(w.conc)
+    ktab, _ = s.rate_constants(conc, d(w.temp), d(w.rho), d(w.rh), None, d(w.param))
+    for r in EXTREME:
+        ktab[r] = torch.clamp(ktab[r], max=1e3)
+    _, dk = o.rate_constants(w.conc, w.temp, w.rho, w.rh, None, w.param)
+    log = s.integrate_logged(conc, ktab, w.dt, log_cap=8192)
+    torch.cuda.synchronize()
+    ln = log["log_n"].cpu().numpy()
+    ok = (log["status"].cpu().numpy() == 0) & (ln < 8192)
+    rep = o.integrate(w.conc.copy(), w.dt, k=ktab.cpu().numpy(), dk=dk, temp=w.temp, rho=w.rho, rh=w.rh,
+                      param=w.param, replay=(log["log_h"].cpu().numpy(), log["log_acc"].cpu().numpy(), ln))
+    ok &= rep["status"] == 0
+    assert ok.mean() > 0.9
+    got, ref = conc.cpu().numpy()[:, ok], rep["conc"][:, ok]
+    atol = np.array(o.raw["atol"])[:, None]
+    assert (np.abs(got - ref) / (np.abs(ref) + atol)).max() <= 1e-9
+
+
+def test_cooperative_handoff_is_bit_identical(lib):
+    import torch
+
+    w, s, o, d = _setup()
+    outs = []
+    try:
+        for defer in (0, 7):
+            s.set_tuning(defer_after=defer)
+            conc = d(w.conc)
+            st, acc, rej = s.integrate(conc, w.dt, temp=d(w.temp), rho=d(w.rho), rh=d(w.rh), param=d(w.param),
+                                       mode="persistent")
+            torch.cuda.synchronize()
+            outs.append((conc.cpu().numpy(), st.cpu().numpy(), acc.cpu().numpy(), rej.cpu().numpy()))
+    finally:
+        s.set_tuning(defer_after=0)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b, equal_nan=True)

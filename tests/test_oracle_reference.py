@@ -13,7 +13,9 @@ These tests compare the oracle port with that build on seeded inputs:
   where a one-ulp difference in k moves the solution by 1e-6 and can change
   the accepted step sequence.  There the bound is statistical, the same two
   bounds the GPU parity tests use for the shipped rates: median to
-  round-off, every cell within 1e-2.
+  round-off, every cell within 1e-2.  saprc99_mini and saprcnov, which the
+  reference also ships, carry the same rates and get the same form of
+  bound (F and J to round-off, integrate() statistically).
 
 Skipped when the reference build is absent (no reference checkout and no
 previously generated headers).
@@ -29,16 +31,19 @@ from oracle.oracle import Oracle
 
 def _ref(mech):
     try:
-        ref_build.build_if_available()
+        if mech in ref_build.MECHS:
+            ref_build.build_if_available()
+            solver = ref_build.load(mech)
+        else:
+            solver = ref_build.ensure(mech)
     except Exception as e:  # pragma: no cover - toolchain problems surface as skips
         pytest.skip(f"reference build failed: {e}")
-    solver = ref_build.load(mech)
     if solver is None:
         pytest.skip("reference solver library not built")
     return solver
 
 
-@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99"])
+@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99", "saprc99_mini", "saprcnov"])
 def test_tendencies_and_jacobian_match_reference(mech):
     ref = _ref(mech)
     o = Oracle(mech)
@@ -74,10 +79,21 @@ def test_integrate_matches_reference(mech):
     assert rel.max() < 1e-12
 
 
-def test_integrate_matches_reference_saprc99_statistically():
-    ref = _ref("saprc99")
-    o = Oracle("saprc99")
-    w = workloads.make("saprc99", 64)
+# Bounds per mechanism, from seeded 64-cell samples (measured: element median
+# 1e-13 / 2e-16 / 3e-14; a quarter of the cells within 4e-13 / 7e-8 / 1e-9;
+# worst cell 5e-3 / 2.4e-2 / 7.5e-3).  All three carry the shipped Troe rates
+# of 1e33-1e37 1/s (saprc99 reactions 11, 32, 69; saprc99_mini 7; saprcnov
+# 10, 31, 57), which amplify one-ulp differences in k.
+SAPRC_BOUNDS = {"saprc99": (1e-11, 1e-11, 1e-2), "saprc99_mini": (1e-11, 1e-6, 5e-2),
+                "saprcnov": (1e-11, 1e-8, 2e-2)}
+
+
+@pytest.mark.parametrize("mech", list(SAPRC_BOUNDS))
+def test_integrate_matches_reference_statistically(mech):
+    med, q25, worst = SAPRC_BOUNDS[mech]
+    ref = _ref(mech)
+    o = Oracle(mech)
+    w = workloads.make(mech, 64)
     a, b = w.conc.copy(), w.conc.copy()
     P = w.param_at(0)
     ro = o.integrate(a, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
@@ -85,12 +101,10 @@ def test_integrate_matches_reference_saprc99_statistically():
     both = (ro["status"] == 0) & np.isfinite(rr["conc"]).all(axis=0)
     assert both.mean() > 0.9
     rel = np.abs(ro["conc"] - rr["conc"]) / np.maximum(np.abs(rr["conc"]), 1.0)
-    # Seeded sample (64 cells): element median 1e-13, a quarter of the cells
-    # to round-off, the worst cell 5e-3.
-    assert np.median(rel[:, both]) < 1e-11
+    assert np.median(rel[:, both]) < med
     per_cell = rel[:, both].max(axis=0)
-    assert np.quantile(per_cell, 0.25) < 1e-11
-    assert per_cell.max() < 1e-2
+    assert np.quantile(per_cell, 0.25) < q25
+    assert per_cell.max() < worst
     # A cell the reference leaves non-finite is one the port flags.
     bad_ref = ~np.isfinite(rr["conc"]).all(axis=0)
     assert np.all(ro["status"][bad_ref] != 0)

@@ -9,7 +9,7 @@ from mkpp_gb300.emitter import cuda_emitter
 from mkpp_gb300.emitter.plan import jacobian_pattern, load, load_raw
 
 GOLD = Path(__file__).resolve().parent / "golden"
-MECHS = ["chapman", "small_strato", "saprc99", "ts1"]
+MECHS = ["chapman", "small_strato", "saprc99", "ts1", "saprc99_mini", "saprcnov"]
 
 
 def _tables(raw):
@@ -59,7 +59,7 @@ def test_reduced_plan_invariants(mech):
     assert written == set(range(len(p.lu_slots)))
 
 
-@pytest.mark.parametrize("mech", ["chapman", "small_strato", "saprc99", "ts1"])
+@pytest.mark.parametrize("mech", MECHS)
 def test_generated_header_is_current(mech):
     plan = load(mech)
     text = cuda_emitter.emit_mechanism(plan)
