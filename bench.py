@@ -325,7 +325,7 @@ def main():
     achieved = flops_run / (kernel_avg_ms * 1e-3) / 1e12 if kernel_ms else None
 
     # Live FP64 FMA peak (DFMA probe on this GPU).
-    probe = C.CDLL(str(ROOT / "mkpp_gb300" / "lib" / "libmkpp_probe.so"))
+    probe = C.CDLL(str(ROOT / "mkpp_gb300" / "lib" / "libgb300_fp64_probe.so"))
     probe.mkpp_probe_fp64_fma.restype = C.c_double
     probe.mkpp_probe_fp64_fma.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
     sms = torch.cuda.get_device_properties(dev).multi_processor_count

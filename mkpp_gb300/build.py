@@ -127,7 +127,7 @@ def compile_mechanism(mech: str, verbose: bool = False, extra: list[str] | None 
 
 
 def compile_probe() -> Path:
-    out = LIB / "libmkpp_probe.so"
+    out = LIB / "libgb300_fp64_probe.so"
     src = CSRC / "probe.cu"
     if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
         return out

@@ -1,0 +1,105 @@
+"""The C++ host registry (include/mkpp_host/mechanism_manager.hpp).
+
+It mirrors the reference's MechanismRegistry and HostExecutionParams
+(src/mkpp_host/include/mkpp_host/mechanism_manager.hpp:21-228,
+dispatcher.hpp:15-254) over the mechanism libraries.  Checked through
+tests/registry/registry_check.cpp:
+* on the CPU: the registered mechanisms are the libraries built; get_info
+  reports the library's sizes; an unknown name, a per-cell extent that does
+  not match the state and too few forcing slots raise the reference's
+  "FATAL ERROR" messages as std::runtime_error / std::invalid_argument;
+* on the GPU: execute() with per-cell meteorology and forcing ends
+  bit-identical to the C ABI driven from Python on the same inputs.
+"""
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+LIB = ROOT / "mkpp_gb300" / "lib"
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from mkpp_gb300 import build
+
+    try:
+        build.build(("chapman", "small_strato"))
+    except RuntimeError as e:  # no nvcc
+        pytest.skip(str(e))
+    exe = tmp_path_factory.mktemp("registry") / "registry_check"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
+                    str(ROOT / "tests" / "registry" / "registry_check.cpp"), "-ldl", "-o", str(exe)], check=True)
+    return exe
+
+
+def _run(exe, *args):
+    return subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True,
+                          env={"MKPP_GB300_LIB_DIR": str(LIB), "PATH": "/usr/bin:/bin"})
+
+
+def test_registered_mechanisms_are_the_built_libraries(checker):
+    out = _run(checker, "list")
+    assert out.returncode == 0, out.stderr
+    built = sorted(p.name[len("libmkpp_"):-len(".so")] for p in LIB.glob("libmkpp_*.so"))
+    assert out.stdout.split() == built
+    assert {"chapman", "small_strato"} <= set(built)
+
+
+def test_get_info_reports_library_sizes(checker):
+    from mkpp_gb300.emitter.plan import load_raw
+
+    for mech in ("chapman", "small_strato"):
+        out = _run(checker, "info", mech)
+        assert out.returncode == 0, out.stderr
+        raw = load_raw(mech)
+        assert out.stdout.split() == [mech, str(len(raw["species"])), str(raw["num_reactions"]), "0"]
+
+
+def test_unknown_mechanism_is_a_fatal_runtime_error(checker):
+    out = _run(checker, "unknown", "no_such_mechanism")
+    assert out.returncode == 3
+    assert out.stdout.startswith("FATAL ERROR: Unknown mechanism 'no_such_mechanism'. Supported: ")
+    assert "chapman" in out.stdout
+
+
+def test_extent_checks_raise_invalid_argument(checker):
+    out = _run(checker, "extent", "chapman")
+    assert out.returncode == 3
+    assert out.stdout.strip() == "FATAL ERROR: per-cell meteorology extent does not match state"
+    out = _run(checker, "forcing", "chapman")
+    assert out.returncode == 3
+    assert out.stdout.strip() == "FATAL ERROR: per-cell forcing has too few runtime parameters"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mech", ["chapman", "small_strato"])
+def test_execute_matches_c_abi(checker, mech, tmp_path):
+    from mkpp_gb300 import workloads
+    from mkpp_gb300.api import MechanismContext
+
+    n, steps = 256, 2
+    w = workloads.make(mech, n)
+    for name, a in (("conc", w.conc), ("temp", w.temp), ("rho", w.rho), ("rh", w.rh), ("param", w.param)):
+        np.ascontiguousarray(a, dtype=np.float64).tofile(tmp_path / f"{name}.bin")
+    out = _run(checker, "execute", mech, n, repr(w.dt), steps, tmp_path)
+    assert out.returncode == 0, out.stderr
+    got = np.fromfile(tmp_path / "conc_out.bin").reshape(w.conc.shape)
+    status = np.fromfile(tmp_path / "status.bin", dtype=np.int32)
+    ref = np.ascontiguousarray(w.conc.copy())
+    ctx = MechanismContext(mech, n)
+    try:
+        ctx.set_state(ref, w.temp.copy(), np.full(n, 101325.0), w.rho.copy())
+        ctx.set_aerosol(relative_humidity=w.rh.copy())
+        ctx.set_rate_parameters(np.ascontiguousarray(w.param))
+        for _ in range(steps):
+            ctx.integrate(w.dt)
+    finally:
+        ctx.close()
+    assert np.array_equal(got, ref, equal_nan=True)
+    assert (status == 0).all()
