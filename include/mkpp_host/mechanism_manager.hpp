@@ -7,7 +7,10 @@
 //   mkpp::host::BasicHostExecutionParams / HostExecutionParams
 //                           src/mkpp_host/include/mkpp_host/dispatcher.hpp:79-97
 //   mkpp::host::CellErrorCode   dispatcher.hpp:15-21
+//   mkpp::host::BatchErrorStatus   dispatcher.hpp:124-144
 //   the per-cell gather of ParamsTiledCellIntegrator   dispatcher.hpp:196-254
+//   mkpp::host::execute_mechanism_steps[_batched], execute_mechanism
+//                           dispatcher.hpp:319-384
 //
 // Differences, all forced by the absence of Kokkos on this side:
 // * Views become pointers with extents (CellValues, CellForcing) and the state
@@ -23,6 +26,9 @@
 // * get_info() reports the mechanism's reaction count (the reference leaves
 //   it 0).  requires_env is false for every library built here: it is true in
 //   the reference only for its equilibrium mechanism, which is not built.
+// * The batched status holds every per-cell outcome of the solve (attempt cap,
+//   numerical failure), not only the non-finite inputs the reference records;
+//   team_size is accepted and unused (the GPU kernels size their own grids).
 //
 // Header-only, C++17; link with -ldl.
 #pragma once
@@ -53,6 +59,16 @@ enum CellErrorCode : int {
   ERR_NON_FINITE_STATE = MKPP_CELL_ERR_NON_FINITE_STATE,
   ERR_CONVERGENCE_FAILURE = MKPP_CELL_ERR_CONVERGENCE,
   ERR_NUMERICAL_FAILURE = MKPP_CELL_ERR_NUMERICAL
+};
+
+template <typename MemorySpace = void>
+struct BatchErrorStatus {
+  std::vector<int> status;
+
+  BatchErrorStatus() = default;
+  explicit BatchErrorStatus(std::size_t num_cells) : status(num_cells, SUCCESS) {}
+  void set_error(std::size_t cell_idx, CellErrorCode code) { status[cell_idx] = static_cast<int>(code); }
+  int get_error(std::size_t cell_idx) const { return status[cell_idx]; }
 };
 
 struct MechanismInfo {
@@ -287,6 +303,51 @@ class MechanismRegistry {
     if (cell_status) std::copy(status.begin(), status.end(), cell_status);
   }
 };
+
+// `steps` integrate() calls of dt on every cell, with one parameter row
+// shared by all cells (null: zeros).
+inline void execute_mechanism_steps(const std::string& name, double* state, std::size_t num_cells, double dt,
+                                    int steps, const double* jvals = nullptr, std::size_t jvals_count = 0) {
+  HostExecutionParams p;
+  p.dt = dt;
+  p.steps = steps;
+  p.jvals = jvals;
+  p.jvals_count = jvals_count;
+  MechanismRegistry::execute(name, state, num_cells, p);
+}
+
+inline void execute_mechanism(const std::string& name, double* state, std::size_t num_cells, double dt,
+                              const double* jvals = nullptr, std::size_t jvals_count = 0) {
+  execute_mechanism_steps(name, state, num_cells, dt, 1, jvals, jvals_count);
+}
+
+// As execute_mechanism_steps, with fault isolation: a cell with a non-finite
+// input is left untouched and flagged ERR_NON_FINITE_STATE, every other cell
+// integrates, and one summary line goes to stderr when any cell faulted.
+template <typename MemorySpace>
+void execute_mechanism_steps_batched(const std::string& name, double* state, std::size_t num_cells, double dt,
+                                     int steps, const double* jvals, std::size_t jvals_count,
+                                     BatchErrorStatus<MemorySpace>& error_status, int team_size = 64) {
+  (void)team_size;
+  if (error_status.status.size() < num_cells) {
+    std::string err = "FATAL ERROR: batched integration error buffer (" + std::to_string(error_status.status.size()) +
+                      ") smaller than batch (" + std::to_string(num_cells) + ").";
+    std::cerr << err << std::endl;
+    throw std::runtime_error(err);
+  }
+  HostExecutionParams p;
+  p.dt = dt;
+  p.steps = steps;
+  p.jvals = jvals;
+  p.jvals_count = jvals_count;
+  MechanismRegistry::execute(name, state, num_cells, p, error_status.status.data());
+  std::size_t faulted = 0;
+  for (std::size_t c = 0; c < num_cells; ++c) faulted += error_status.status[c] != SUCCESS;
+  if (faulted > 0) {
+    std::cerr << "FATAL ERROR: batched integration of '" << name << "' reported " << faulted << " faulted cell(s) of "
+              << num_cells << "; per-cell codes are in the status buffer\n";
+  }
+}
 
 }  // namespace host
 }  // namespace mkpp

@@ -8,6 +8,9 @@
 //   registry_check execute <m> <n> <dt> <steps> <dir>
 //       reads <dir>/{conc,temp,rho,rh,param}.bin (float64, LayoutLeft), runs
 //       execute(), writes <dir>/{conc_out,status}.bin
+//   registry_check batched <m> <n> <dt> <steps> <dir>
+//       reads <dir>/{conc,jvals}.bin, runs execute_mechanism_steps_batched()
+//       with the shared parameter row, writes <dir>/{conc_out,status}.bin
 // The error modes print the exception's message and exit 3 when it is the
 // expected kind, 1 otherwise.
 #include <cstdio>
@@ -100,6 +103,25 @@ int main(int argc, char** argv) {
     MechanismRegistry::execute(mech, conc.data(), n, p, status.data());
     write(dir + "/conc_out.bin", conc);
     write(dir + "/status.bin", status);
+    return 0;
+  }
+  if (mode == "batched" && argc == 7) {
+    const size_t n = std::stoul(argv[3]);
+    const double dt = std::stod(argv[4]);
+    const int steps = std::stoi(argv[5]);
+    const std::string dir = argv[6];
+    const auto info = MechanismRegistry::get_info(mech);
+    size_t np = 0;
+    {
+      std::ifstream f(dir + "/jvals.bin", std::ios::binary | std::ios::ate);
+      np = static_cast<size_t>(f.tellg()) / sizeof(double);
+    }
+    auto conc = read(dir + "/conc.bin", n * info.num_species);
+    auto jvals = np ? read(dir + "/jvals.bin", np) : std::vector<double>();
+    mkpp::host::BatchErrorStatus<> err(n);
+    mkpp::host::execute_mechanism_steps_batched(mech, conc.data(), n, dt, steps, jvals.data(), np, err);
+    write(dir + "/conc_out.bin", conc);
+    write(dir + "/status.bin", err.status);
     return 0;
   }
   return 2;

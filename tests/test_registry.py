@@ -9,8 +9,13 @@ tests/registry/registry_check.cpp:
   not match the state and too few forcing slots raise the reference's
   "FATAL ERROR" messages as std::runtime_error / std::invalid_argument;
 * on the GPU: execute() with per-cell meteorology and forcing ends
-  bit-identical to the C ABI driven from Python on the same inputs.
+  bit-identical to the C ABI driven from Python on the same inputs, and the
+  batched path (execute_mechanism_steps_batched) leaves a cell with a NaN
+  input untouched, flags it ERR_NON_FINITE_STATE (2), prints one summary
+  line and integrates the others as the C ABI does
+  (test_e2e_batched.cpp's NaN isolation).
 """
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -40,7 +45,7 @@ def checker(tmp_path_factory):
 
 def _run(exe, *args):
     return subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True,
-                          env={"MKPP_GB300_LIB_DIR": str(LIB), "PATH": "/usr/bin:/bin"})
+                          env={**os.environ, "MKPP_GB300_LIB_DIR": str(LIB)})
 
 
 def test_registered_mechanisms_are_the_built_libraries(checker):
@@ -103,3 +108,34 @@ def test_execute_matches_c_abi(checker, mech, tmp_path):
         ctx.close()
     assert np.array_equal(got, ref, equal_nan=True)
     assert (status == 0).all()
+
+
+@pytest.mark.gpu
+def test_batched_path_isolates_non_finite_cell(checker, tmp_path):
+    from mkpp_gb300 import workloads
+    from mkpp_gb300.api import MechanismContext
+
+    mech, n, steps, bad = "chapman", 64, 1, 5
+    w = workloads.make(mech, n)
+    conc = np.ascontiguousarray(w.conc.copy())
+    conc[0, bad] = np.nan
+    jvals = np.ascontiguousarray(w.param[:, 0])
+    conc.tofile(tmp_path / "conc.bin")
+    jvals.tofile(tmp_path / "jvals.bin")
+    out = _run(checker, "batched", mech, n, repr(w.dt), steps, tmp_path)
+    assert out.returncode == 0, out.stderr
+    assert f"reported 1 faulted cell(s) of {n}" in out.stderr
+    got = np.fromfile(tmp_path / "conc_out.bin").reshape(conc.shape)
+    status = np.fromfile(tmp_path / "status.bin", dtype=np.int32)
+    assert status[bad] == 2 and (np.delete(status, bad) == 0).all()
+    assert np.array_equal(got[:, bad], conc[:, bad], equal_nan=True)
+    ref = conc.copy()
+    ctx = MechanismContext(mech, n)
+    try:
+        ctx.set_state(ref, np.full(n, 288.15), np.full(n, 101325.0), np.full(n, 2.4476e19))
+        ctx.set_aerosol(relative_humidity=np.full(n, 0.5))
+        ctx.set_rate_parameters(np.ascontiguousarray(np.repeat(jvals[:, None], n, axis=1)))
+        ctx.integrate(w.dt)
+    finally:
+        ctx.close()
+    assert np.array_equal(got, ref, equal_nan=True)
