@@ -1,0 +1,71 @@
+"""Static invariants of the device code (no GPU needed).
+
+The reference checks its generated solvers for GPU safety by reading the
+generated code (tests/python/test_gpu_safety_all_solvers.py: no heap
+allocation, fully unrolled stages).  The same kind of checks here, over the
+emitted headers (mkpp_gb300/generated/*.cuh) and the hand-written device
+code (csrc/solver.cuh, csrc/mkpp_device.cuh):
+* no heap allocation, device printf, trap or device assert;
+* the emitted per-mechanism code has no while loop: every loop has a
+  compile-time trip count or walks a table of known length;
+* every controller loop is bounded by the attempt cap, and no device loop
+  waits on memory another thread writes, so no kernel can spin forever.
+"""
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+GENERATED = sorted((ROOT / "mkpp_gb300" / "generated").glob("*.cuh"))
+HANDWRITTEN = [ROOT / "mkpp_gb300" / "csrc" / f for f in ("solver.cuh", "mkpp_device.cuh")]
+FORBIDDEN = (r"\bmalloc\s*\(", r"\bcalloc\s*\(", r"\brealloc\s*\(", r"\bfree\s*\(", r"\bnew\s+\w",
+             r"\bdelete\b", r"\bprintf\s*\(", r"__trap\s*\(", r"\bassert\s*\(", r"\btrap\s*;",
+             r"__nanosleep\s*\(")
+
+
+def _code(path):
+    """The file without comments and string literals."""
+    text = path.read_text()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    return re.sub(r'"(?:\\.|[^"\\])*"', '""', text)
+
+
+def test_the_files_exist():
+    assert len(GENERATED) >= 4 and all(p.exists() for p in HANDWRITTEN)
+
+
+@pytest.mark.parametrize("path", GENERATED + HANDWRITTEN, ids=lambda p: p.name)
+def test_no_allocation_print_or_trap_in_device_code(path):
+    code = _code(path)
+    for pat in FORBIDDEN:
+        assert not re.search(pat, code), (path.name, pat)
+
+
+@pytest.mark.parametrize("path", GENERATED, ids=lambda p: p.name)
+def test_emitted_code_has_no_while_loop(path):
+    assert not re.search(r"\bwhile\s*\(", _code(path))
+
+
+def test_controller_loops_are_bounded_by_the_attempt_cap():
+    code = _code(ROOT / "mkpp_gb300" / "csrc" / "solver.cuh")
+    loops = [m.end() for m in re.finditer(r"while\s*\(\s*ctl\.running\(\)\s*\)\s*\{", code)]
+    assert loops
+    for end in loops:
+        body = code[end:end + 200]
+        assert re.match(r"\s*if\s*\(\s*ctl\.attempts\s*>=\s*a\.max_attempts\s*\)", body), body[:120]
+    # The other loops: fixed trip counts, grid-stride over cells, or the
+    # persistent work loop, which ends when the queue is drained and every
+    # lane's cell is done.
+    whiles = len(re.findall(r"\bwhile\s*\(", code))
+    assert whiles == len(loops), (whiles, len(loops))
+    assert len(re.findall(r"for\s*\(\s*;\s*;\s*\)", code)) == 1
+    assert "if (__ballot_sync(0xffffffffu, active) == 0u) break;" in code
+
+
+@pytest.mark.parametrize("path", HANDWRITTEN, ids=lambda p: p.name)
+def test_no_device_loop_polls_memory(path):
+    code = _code(path)
+    assert not re.search(r"\bvolatile\b", code)
+    assert not re.search(r"atomicCAS\s*\(", code)
