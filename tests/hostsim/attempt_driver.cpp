@@ -1,7 +1,7 @@
-// One Rosenbrock attempt, and the adjoint of one step, of an emitted mechanism
-// header on the host (TEST INFRASTRUCTURE ONLY).  The store is a plain array of the per-cell slots
-// (the layout of Mech: Y, stage vectors K0.., F, DY, KT), the rate constants
-// a plain array.
+// The rate constants, one Rosenbrock attempt, and the adjoint and tangent of
+// one step, of an emitted mechanism header on the host (TEST INFRASTRUCTURE
+// ONLY).  The store is a plain array of the per-cell slots (the layout of
+// Mech: Y, stage vectors K0.., F, DY, KT), the rate constants a plain array.
 #include MKPP_MECH_HEADER
 
 namespace {
@@ -16,9 +16,28 @@ struct Rates {
   const double* k;
   double operator()(int r) const { return k[r]; }
 };
+
+struct Row {
+  const double* v;
+  double operator()(int i) const { return v ? v[i] : 0.0; }
+};
+
+struct RowOut {
+  double* v;
+  void set(int i, double x) const { v[i] = x; }
+};
 }  // namespace
 
 extern "C" {
+
+// Rate constants of one cell from the emitted rate_constants(): conc holds
+// the cell's NS concentrations (the fixed species are read), param its
+// runtime parameters (null: zeros); k receives NR values.
+void hostsim_rate_constants(const double* conc, const double* param, double T, double RHO, double RH, double CLW,
+                            double* k) {
+  RowOut out{k};
+  Mech::rate_constants(Row{param}, Row{conc}, T, RHO, RH, CLW, out);
+}
 
 // NSLOTS, NV, NR, NSTAGE, Y, K0, F, DY, KT
 int hostsim_layout(int* out) {

@@ -407,3 +407,26 @@ def test_tangent_taylor_test(hostsim, mech):
         r.append(np.max(np.abs(Ye - Y - e * T) / scale))
     ratios = np.array(r[:-1]) / np.array(r[1:])
     assert np.all((ratios > 3.9) & (ratios < 4.1)), ratios
+
+
+@pytest.mark.parametrize("mech", MECHS + EXTRA + ["ts1"])
+def test_emitted_rate_constants_match_oracle(hostsim, mech):
+    """The emitted rate_constants() (the code rate_constant_kernel runs),
+    compiled for the host, against the oracle's rate constants on seeded
+    cells: 1e-13 relative (glibc vs numpy exp/log/pow).  This pins the
+    emitted expressions, their parameter-slot, fixed-species and
+    environment arguments for every mechanism, TS1's 547 included."""
+    lib = hostsim[mech]
+    lib.hostsim_rate_constants.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_void_p]
+    n = 16
+    w = workloads.make(mech, n)
+    o = Oracle(mech)
+    k_ref, _ = o.rate_constants(w.conc, w.temp, w.rho, w.rh, None, w.param)
+    for c in range(n):
+        conc = np.ascontiguousarray(w.conc[:, c])
+        prm = np.ascontiguousarray(w.param[:, c]) if w.param.shape[0] else None
+        k = np.zeros(k_ref.shape[0])
+        lib.hostsim_rate_constants(conc.ctypes.data, None if prm is None else prm.ctypes.data, w.temp[c],
+                                   w.rho[c], w.rh[c], 0.0, k.ctypes.data)
+        np.testing.assert_allclose(k, k_ref[:, c], rtol=1e-13, atol=0)
