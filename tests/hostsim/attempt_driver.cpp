@@ -26,6 +26,36 @@ struct RowOut {
   double* v;
   void set(int i, double x) const { v[i] = x; }
 };
+
+// Tendencies F[s] and the dense Jacobian J[row + NS * col] of one cell from
+// the emitted fun(), jac_w() (with 1/(gamma h) = 0, negated) and
+// jac_fixed_columns(), composed as the evaluation kernels compose them.
+// A table-driven mechanism has none of the three: returns -1.
+template <class M>
+int evaluate(const double* conc, const double* param, double T, double RHO, double RH, double CLW,
+             const double* k, double* F, double* J) {
+  if constexpr (M::TABLE_ATTEMPT) {
+    return -1;
+  } else {
+    const int NS = M::NS;
+    struct Y {
+      const double* c;
+      double operator()(int i) const { return c[M::var_phys(i)]; }
+    } y{conc};
+    struct Dense {
+      double* J;
+      double& operator[](int s) const { return J[M::lu_prow(s) + M::NS * M::lu_pcol(s)]; }
+    } S{J};
+    for (int s = 0; s < NS; ++s) F[s] = 0.0;
+    for (int e = 0; e < NS * NS; ++e) J[e] = 0.0;
+    M::fun(y, Rates{k}, [&](int i, double v) { F[M::var_phys(i)] = v; });
+    M::jac_w(y, Rates{k}, 0.0, S);
+    M::for_each_w_slot([&](int slot, int, int) { S[slot] = -S[slot]; });
+    M::jac_fixed_columns(Row{param}, Row{conc}, T, RHO, RH, CLW, y,
+                         [&](int row, int col, double v) { J[row + NS * col] = v; });
+    return 0;
+  }
+}
 }  // namespace
 
 extern "C" {
@@ -37,6 +67,13 @@ void hostsim_rate_constants(const double* conc, const double* param, double T, d
                             double* k) {
   RowOut out{k};
   Mech::rate_constants(Row{param}, Row{conc}, T, RHO, RH, CLW, out);
+}
+
+// Tendencies and dense Jacobian of one cell (evaluate() above); -1 for a
+// table-driven mechanism.
+int hostsim_evaluate(const double* conc, const double* param, double T, double RHO, double RH, double CLW,
+                     const double* k, double* F, double* J) {
+  return evaluate<Mech>(conc, param, T, RHO, RH, CLW, k, F, J);
 }
 
 // NSLOTS, NV, NR, NSTAGE, Y, K0, F, DY, KT

@@ -430,3 +430,49 @@ def test_emitted_rate_constants_match_oracle(hostsim, mech):
         lib.hostsim_rate_constants(conc.ctypes.data, None if prm is None else prm.ctypes.data, w.temp[c],
                                    w.rho[c], w.rh[c], 0.0, k.ctypes.data)
         np.testing.assert_allclose(k, k_ref[:, c], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("mech", MECHS + EXTRA)
+def test_emitted_tendencies_and_jacobian_match_reference(hostsim, mech):
+    """The emitted fun(), jac_w() and jac_fixed_columns() (what the GPU
+    evaluation entries run), compiled for the host and fed the emitted rate
+    constants, against the reference's own generated compute_rates /
+    compute_jacobian built here (oracle/ref_build.py): F to 1e-13 of the
+    cell's largest |F|, every nonzero J entry to 1e-11, and zeros wherever the
+    reference writes none.  The two sum the mass-action terms in different
+    orders."""
+    from oracle import ref_build
+
+    try:
+        if mech in ref_build.MECHS:
+            ref_build.build_if_available()
+            ref = ref_build.load(mech)
+        else:
+            ref = ref_build.ensure(mech)
+    except Exception as e:  # noqa: BLE001
+        pytest.skip(f"reference build failed: {e}")
+    if ref is None:
+        pytest.skip("reference solver library not built")
+    lib = hostsim[mech]
+    lib.hostsim_rate_constants.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_void_p]
+    lib.hostsim_evaluate.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_void_p, C.c_void_p, C.c_void_p]
+    n = 16
+    w = workloads.make(mech, n)
+    F0, J0 = ref.evaluate(w.conc, w.temp, w.rho, w.rh, w.param)
+    ns, nr = F0.shape[0], len(load(mech).reactions)
+    for c in range(n):
+        conc = np.ascontiguousarray(w.conc[:, c])
+        prm = np.ascontiguousarray(w.param[:, c]) if w.param.shape[0] else None
+        pp = None if prm is None else prm.ctypes.data
+        k = np.zeros(nr)
+        lib.hostsim_rate_constants(conc.ctypes.data, pp, w.temp[c], w.rho[c], w.rh[c], 0.0, k.ctypes.data)
+        F, J = np.zeros(ns), np.zeros(ns * ns)
+        assert lib.hostsim_evaluate(conc.ctypes.data, pp, w.temp[c], w.rho[c], w.rh[c], 0.0, k.ctypes.data,
+                                    F.ctypes.data, J.ctypes.data) == 0
+        J = J.reshape(ns, ns).T                       # [row, col]
+        assert np.abs(F - F0[:, c]).max() <= 1e-13 * max(np.abs(F0[:, c]).max(), 1e-300)
+        nz = J0[:, :, c] != 0
+        assert not np.any(J[~nz])
+        assert (np.abs(J - J0[:, :, c])[nz] / np.abs(J0[:, :, c][nz])).max() < 1e-11
