@@ -296,19 +296,12 @@ int mkpp_create_handle(mkpp_handle_t* handle_out, size_t num_cells) {
   return MKPP_SUCCESS;
 }
 
+// Frees what the handle allocated; a handle that never computed makes no
+// CUDA call here.
 static void free_device(DeviceBuffers& d) {
-  cudaFree(d.conc);
-  cudaFree(d.temp);
-  cudaFree(d.rho);
-  cudaFree(d.rh);
-  cudaFree(d.clw);
-  cudaFree(d.param);
-  cudaFree(d.ktab);
-  cudaFree(d.out);
-  cudaFree(d.status);
-  cudaFree(d.accepted);
-  cudaFree(d.rejected);
-  cudaFree(d.workspace);
+  for (void* p : {(void*)d.conc, (void*)d.temp, (void*)d.rho, (void*)d.rh, (void*)d.clw, (void*)d.param,
+                  (void*)d.ktab, (void*)d.out, (void*)d.status, (void*)d.accepted, (void*)d.rejected, d.workspace})
+    if (p) cudaFree(p);
   d = DeviceBuffers();
 }
 
@@ -320,12 +313,11 @@ int mkpp_destroy_handle(mkpp_handle_t handle) {
   return MKPP_SUCCESS;
 }
 
+// Like the reference's, initialization only readies the handle: the stream
+// and the device buffers are created by the first call that computes, so a
+// host without a GPU gets MKPP_ERROR_DEVICE there, with a message.
 int mkpp_initialize(mkpp_handle_t handle) {
   if (!handle) return MKPP_ERROR_NULL_POINTER;
-  if (!handle->stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&handle->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return device_fail(handle, e, "cudaStreamCreateWithFlags");
-  }
   handle->initialized = true;
   return MKPP_SUCCESS;
 }
@@ -442,6 +434,7 @@ int mkpp_set_aerosol_ptrs(mkpp_handle_t handle, const double* relative_humidity,
 static int ensure_device(mkpp_handle_s* h, size_t out_bytes) {
   DeviceBuffers& d = h->dev;
   const size_t n = h->num_cells;
+  if (!h->stream) MKPP_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   if (d.cells != n) {
     free_device(d);
     MKPP_CUDA(h, cudaMalloc(&d.conc, n * Mech::NS * sizeof(double)));

@@ -1,0 +1,131 @@
+"""C-ABI lifecycle and argument contract, on any host (no GPU needed).
+
+The reference's contract tests (tests/contract/test_c_abi.cpp:9-80) check the
+handle lifecycle, state binding and error codes of the generated mkpp.h.
+The same calls against libmkpp_chapman.so, plus the argument checks that
+return before any device work (src/mkpp/templates/host_api/
+mkpp_c_api.cpp.j2:70-374 gives the codes):
+* null handles and pointers: MKPP_ERROR_NULL_POINTER (-101);
+* zero cells, a wrong parameter count, dt <= 0, a non-positive temperature:
+  MKPP_ERROR_INVALID_ARGUMENT (-103), with a "FATAL ERROR" message;
+* integrate or evaluate before initialization, statistics before any
+  integration: MKPP_ERROR_INVALID_STATE (-104);
+* an unknown species name: MKPP_ERROR_NOT_FOUND (-106).
+Initialization makes no CUDA call, as the reference's makes no device call.
+The first call that computes does: on a host without a GPU it fails loudly
+with MKPP_ERROR_DEVICE (-107) and the CUDA runtime's reason (there is no CPU
+fallback); on a GB300 it succeeds.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+MECH = "chapman"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mkpp_gb300 import api, build
+
+    try:
+        build.build((MECH,))
+    except RuntimeError as e:  # no nvcc
+        pytest.skip(str(e))
+    return api.load_library(MECH)
+
+
+def _handle(lib, n):
+    h = C.c_void_p()
+    assert lib.mkpp_create_handle(C.byref(h), n) == 0
+    assert h.value
+    return h
+
+
+def _error(lib, h):
+    buf = C.create_string_buffer(512)
+    assert lib.mkpp_get_last_error(h, buf, 512) == 0
+    return buf.value.decode()
+
+
+def _gpu():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:  # noqa: BLE001
+        return False
+
+
+def test_handle_lifecycle_and_metadata(lib):
+    assert lib.mkpp_initialize(None) == -101
+    h = C.c_void_p()
+    assert lib.mkpp_create_handle(None, 10) == -101
+    assert lib.mkpp_create_handle(C.byref(h), 0) == -103
+    h = _handle(lib, 10)
+    assert lib.mkpp_initialize(h) == 0
+    count = C.c_size_t()
+    assert lib.mkpp_get_species_count(h, C.byref(count)) == 0 and count.value == 4
+    assert lib.mkpp_get_reaction_count(h, C.byref(count)) == 0 and count.value == 4
+    assert lib.mkpp_get_photolysis_count(h, C.byref(count)) == 0 and count.value == 2
+    assert lib.mkpp_get_species_count(h, None) == -101
+    idx = C.c_int(-1)
+    assert lib.mkpp_get_species_index(h, b"O3", C.byref(idx)) == 0 and idx.value == 2
+    assert lib.mkpp_get_species_index(h, b"XYZ", C.byref(idx)) == -106
+    assert lib.mkpp_destroy_handle(h) == 0
+    assert lib.mkpp_destroy_handle(None) == -101
+
+
+def test_state_binding_and_argument_errors(lib):
+    n = 5
+    h = _handle(lib, n)
+    try:
+        conc = np.full((4, n), 1e9)
+        t, p, rho = np.full(n, 298.15), np.full(n, 101325.0), np.full(n, 2.45e19)
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+        # Before initialization.
+        assert lib.mkpp_set_state_ptrs(h, ptr(conc), ptr(t), ptr(p), ptr(rho)) == 0
+        assert lib.mkpp_integrate(h, C.c_double(60.0)) == -104
+        assert "initialized" in _error(lib, h)
+        assert lib.mkpp_initialize(h) == 0
+        assert lib.mkpp_set_state_ptrs(h, None, ptr(t), ptr(p), ptr(rho)) == -101
+        assert lib.mkpp_set_state_ptrs(h, ptr(conc), ptr(t), ptr(p), ptr(rho)) == 0
+        prm = np.zeros((2, n))
+        assert lib.mkpp_set_rate_parameter_ptrs(h, ptr(prm), 3) == -103
+        assert lib.mkpp_set_rate_parameter_ptrs(h, ptr(prm), 2) == 0
+        rh, sa = np.full(n, 0.7), np.full(n, 1e-4)
+        assert lib.mkpp_set_aerosol_ptrs(h, ptr(rh), ptr(sa)) == 0
+        assert lib.mkpp_set_cloud_water_ptr(h, ptr(np.zeros(n))) == 0
+        status = np.zeros(n, np.int32)
+        assert lib.mkpp_get_cell_stats(h, ptr(status), None, None) == -104
+        assert lib.mkpp_integrate(h, C.c_double(0.0)) == -103
+        assert lib.mkpp_integrate(h, C.c_double(float("nan"))) == -103
+        t[2] = 0.0
+        assert lib.mkpp_integrate(h, C.c_double(60.0)) == -103
+        assert _error(lib, h).startswith("FATAL ERROR: cell temperature")
+        t[2] = 298.15
+        assert lib.mkpp_evaluate_rates(h, None) == -101
+        assert lib.mkpp_evaluate_jacobian(h, None) == -101
+    finally:
+        assert lib.mkpp_destroy_handle(h) == 0
+
+
+def test_compute_without_a_gpu_fails_loudly(lib):
+    n = 4
+    h = _handle(lib, n)
+    try:
+        conc = np.full((4, n), 1e9)
+        t, p, rho = np.full(n, 298.15), np.full(n, 101325.0), np.full(n, 2.45e19)
+        prm = np.zeros((2, n))
+        assert lib.mkpp_initialize(h) == 0
+        assert lib.mkpp_set_state_ptrs(h, conc.ctypes.data, t.ctypes.data, p.ctypes.data, rho.ctypes.data) == 0
+        assert lib.mkpp_set_rate_parameter_ptrs(h, prm.ctypes.data, 2) == 0
+        rc = lib.mkpp_integrate(h, C.c_double(60.0))
+        if _gpu():
+            assert rc == 0
+        else:
+            assert rc == -107
+            assert _error(lib, h).startswith("FATAL ERROR: cudaStreamCreateWithFlags")
+            assert np.all(conc == 1e9)
+    finally:
+        assert lib.mkpp_destroy_handle(h) == 0

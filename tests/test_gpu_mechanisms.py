@@ -127,12 +127,14 @@ def test_heterogeneous_batch_equals_single_cells(lib, built_libs, mech):
                    np.ascontiguousarray(param[:, c:c + 1]))
         assert np.array_equal(r1[:, 0], rates[:, c])
         assert np.array_equal(one[:, 0], batch[:, c])
-    bad = temp.copy()
-    bad[0] = 0.0
+    # As the reference does: bind valid meteorology, then zero a temperature
+    # in the bound array before integrating.
+    t_bound = temp.copy()
     ctx = MechanismContext(mech, n)
     try:
-        ctx.set_state(np.ascontiguousarray(w.conc.copy()), bad, pressure.copy(), rho.copy())
+        ctx.set_state(np.ascontiguousarray(w.conc.copy()), t_bound, pressure.copy(), rho.copy())
         ctx.set_rate_parameters(param)
+        t_bound[0] = 0.0
         with pytest.raises(MkppError) as e:
             ctx.integrate(w.dt)
         assert e.value.code == -103
