@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
     ap.add_argument("--adjoint-cells", type=int, default=65536, help="cells of the adjoint/forward measurement")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--e2e-cost-order", type=int, default=0,
+                    help="e2e handle hands out the previous call's most expensive cells first (mkpp_set_cost_order)")
     return ap.parse_args()
 
 
@@ -467,6 +469,8 @@ def main():
         conc_np, par_np = work_conc.numpy(), [x.numpy() for x in host_par]
         ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
         ctx.set_aerosol(relative_humidity=rh_h.numpy())
+        if args.e2e_cost_order:
+            ctx.set_cost_order(True)
         e2e_times = []
         for rep in range(1):
             work_conc.copy_(host_conc)
@@ -481,7 +485,8 @@ def main():
         h2d = hs * n * 8 * (NS + 3 + NP)
         d2h = hs * n * 8 * NS
         result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                         "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24"}
+                         "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24",
+                         "cost_order": bool(args.e2e_cost_order)}
         ctx.close()
 
     if rank == 0 and world == 1:

@@ -93,6 +93,12 @@ int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts);
 /* Read back the per-cell status / accepted / rejected counts of the last
  * mkpp_integrate (each array num_cells ints; any may be NULL). */
 int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* rejected);
+/* Cost ordering (default off): each mkpp_integrate hands out first the cells
+ * that needed the most attempts in the previous call on this handle, so the
+ * slowest cells start first and the call's tail shrinks.  Results do not
+ * depend on it (cells are independent); it reads back num_cells x 2 ints per
+ * call.  enable 0 turns it off and forgets the counts. */
+int mkpp_set_cost_order(mkpp_handle_t handle, int enable);
 
 /* ---- Mechanism metadata (no reference C entry; compile-time constants of
  * the generated SolverKernels, header.j2:127-186) ------------------------ */

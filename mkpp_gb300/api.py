@@ -85,6 +85,7 @@ SIGNATURES = [
                                            _vp]),
     ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    ("mkpp_set_cost_order", _i, [_vp, _i]),
     ("mkpp_gpu_tangent_workspace_bytes", _sz, [_sz]),
     ("mkpp_gpu_tangent", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_integrate_noalloc", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _vp, _vp, _vp, _vp]),
@@ -226,6 +227,10 @@ class MechanismContext:
 
     def set_max_attempts(self, n: int):
         self._check(self.lib.mkpp_set_max_attempts(self.handle, C.c_int(n)))
+
+    def set_cost_order(self, enable: bool = True):
+        """Hand out the previous call's most expensive cells first."""
+        self._check(self.lib.mkpp_set_cost_order(self.handle, C.c_int(1 if enable else 0)))
 
     # --- compute ---------------------------------------------------------
     def integrate(self, dt: float):

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "capi_common.cuh"
 
@@ -38,6 +39,7 @@ struct DeviceBuffers {
   int* status = nullptr;
   int* accepted = nullptr;
   int* rejected = nullptr;
+  int* order = nullptr;        // queue position -> cell (cost ordering)
   void* workspace = nullptr;
   size_t workspace_bytes = 0;  // grows when a launch-tuning change enlarges the grid
 };
@@ -59,6 +61,12 @@ struct mkpp_handle_s {
   double seed = Mech::SEED;
   int max_attempts = kDefaultMaxAttempts;
   int mode = 1;  // persistent queue
+  // Cost ordering (mkpp_set_cost_order): the persistent queue hands out the
+  // cells that needed the most attempts in the previous call first.
+  bool cost_order = false;
+  std::vector<int> cost;       // attempts per cell of the previous call
+  std::vector<int> rejected;   // staging for the read-back
+  std::vector<int> order;      // queue position -> cell
   cudaStream_t stream = nullptr;
   DeviceBuffers dev;
   std::string last_error;
@@ -300,7 +308,8 @@ int mkpp_create_handle(mkpp_handle_t* handle_out, size_t num_cells) {
 // CUDA call here.
 static void free_device(DeviceBuffers& d) {
   for (void* p : {(void*)d.conc, (void*)d.temp, (void*)d.rho, (void*)d.rh, (void*)d.clw, (void*)d.param,
-                  (void*)d.ktab, (void*)d.out, (void*)d.status, (void*)d.accepted, (void*)d.rejected, d.workspace})
+                  (void*)d.ktab, (void*)d.out, (void*)d.status, (void*)d.accepted, (void*)d.rejected,
+                  (void*)d.order, d.workspace})
     if (p) cudaFree(p);
   d = DeviceBuffers();
 }
@@ -511,13 +520,38 @@ int mkpp_integrate(mkpp_handle_t handle, double dt) {
   if (rc != MKPP_SUCCESS) return rc;
   DeviceBuffers& d = h->dev;
   const size_t n = h->num_cells;
-  rc = launch_integrate(make_args(n, d.conc, d.ktab, 1, dt, h->seed, h->max_attempts, d.status, d.accepted,
-                                  d.rejected),
-                        h->mode, d.workspace, h->stream);
+  mkpp::LaunchArgs args = make_args(n, d.conc, d.ktab, 1, dt, h->seed, h->max_attempts, d.status, d.accepted,
+                                    d.rejected);
+  if (h->cost_order && h->cost.size() == n) {
+    // Most expensive first; ties keep the cell order.
+    h->order.resize(n);
+    for (size_t c = 0; c < n; ++c) h->order[c] = (int)c;
+    std::stable_sort(h->order.begin(), h->order.end(), [h](int x, int y) { return h->cost[x] > h->cost[y]; });
+    if (!d.order) MKPP_CUDA(h, cudaMalloc(&d.order, n * sizeof(int)));
+    MKPP_CUDA(h, cudaMemcpyAsync(d.order, h->order.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    args.order = d.order;
+  }
+  rc = launch_integrate(args, h->mode, d.workspace, h->stream);
   if (rc != MKPP_SUCCESS) return device_fail(h, cudaGetLastError(), "integrate kernel launch");
   MKPP_CUDA(h, cudaMemcpyAsync(h->conc, d.conc, n * Mech::NS * sizeof(double), cudaMemcpyDeviceToHost,
                                h->stream));
+  if (h->cost_order) {
+    h->cost.resize(n);
+    h->rejected.resize(n);
+    MKPP_CUDA(h, cudaMemcpyAsync(h->cost.data(), d.accepted, n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MKPP_CUDA(h, cudaMemcpyAsync(h->rejected.data(), d.rejected, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                 h->stream));
+  }
   MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->cost_order)
+    for (size_t c = 0; c < n; ++c) h->cost[c] += h->rejected[c];
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_cost_order(mkpp_handle_t handle, int enable) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  handle->cost_order = enable != 0;
+  handle->cost.clear();
   return MKPP_SUCCESS;
 }
 

@@ -98,6 +98,8 @@ def test_state_binding_and_argument_errors(lib):
         assert lib.mkpp_set_cloud_water_ptr(h, ptr(np.zeros(n))) == 0
         status = np.zeros(n, np.int32)
         assert lib.mkpp_get_cell_stats(h, ptr(status), None, None) == -104
+        assert lib.mkpp_set_cost_order(None, 1) == -101
+        assert lib.mkpp_set_cost_order(h, 1) == 0 and lib.mkpp_set_cost_order(h, 0) == 0
         assert lib.mkpp_integrate(h, C.c_double(0.0)) == -103
         assert lib.mkpp_integrate(h, C.c_double(float("nan"))) == -103
         t[2] = 0.0

@@ -30,3 +30,31 @@ def test_launch_tuning_change_on_a_live_handle(built_libs):
         s.set_tuning(register_variant=2)
         ctx.close()
     assert np.array_equal(outs[0], outs[1], equal_nan=True)
+
+
+def test_cost_order_leaves_results_unchanged(built_libs):
+    """mkpp_set_cost_order: three host steps through mkpp_integrate with the
+    previous call's most expensive cells handed out first end bit-identical,
+    state and per-cell counts, to the same calls in cell order."""
+    from mkpp_gb300.api import MechanismContext
+
+    w = workloads.make("saprc99", 96)
+    runs = []
+    for enable in (False, True):
+        ctx = MechanismContext("saprc99", w.ncells)
+        try:
+            ctx.set_cost_order(enable)
+            host = np.ascontiguousarray(w.conc.copy())
+            ctx.set_state(host, w.temp.copy(), w.pressure.copy(), w.rho.copy())
+            ctx.set_aerosol(relative_humidity=w.rh.copy())
+            out = []
+            for step in range(3):
+                ctx.set_rate_parameters(np.ascontiguousarray(w.param_at(step)))
+                ctx.integrate(w.dt)
+                out.append((host.copy(), *ctx.cell_stats()))
+            runs.append(out)
+        finally:
+            ctx.close()
+    for a, b in zip(*runs):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y, equal_nan=True)
