@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
     ap.add_argument("--adjoint-cells", type=int, default=65536, help="cells of the adjoint/forward measurement")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--tail-after", type=int, default=0,
+                    help="tail parking threshold in attempts for every integrate launch (mkpp_set_tail_parking; 0 off)")
     ap.add_argument("--e2e-cost-order", type=int, default=0,
                     help="e2e handle hands out the previous call's most expensive cells first (mkpp_set_cost_order)")
     return ap.parse_args()
@@ -237,6 +239,8 @@ def main():
     plan = load(w.mechanism)
     lib = load_library(w.mechanism)
     solver = DeviceSolver(w.mechanism)
+    if args.tail_after:
+        solver.set_tail_parking(args.tail_after)
     NS, NR, NP = solver.sizes.species, solver.sizes.reactions, solver.sizes.rate_parameters
     seed = float(raw["initial_step_seed"])
 
@@ -348,10 +352,12 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
-        "gpu_launches": args.steps * (hs + 1 + (int(os.environ.get("MKPP_DEFER_AFTER", "3000")) > 0)),
+        "gpu_launches": args.steps * (hs + 1 + (int(os.environ.get("MKPP_DEFER_AFTER", "3000")) > 0
+                                                or args.tail_after > 0)),
         "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
                    "defer_after_per_host_step": os.environ.get("MKPP_DEFER_AFTER", "3000"), "cost_order": bool(args.order),
+                   "tail_after": args.tail_after,
                    "max_attempts_per_call": args.max_attempts},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],

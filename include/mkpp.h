@@ -125,6 +125,15 @@ size_t mkpp_gpu_workspace_bytes(size_t num_cells);
  * Results do not depend on it: a handed-off cell ends bit-identical. */
 int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after);
 
+/* Process-wide tail parking of the persistent integrate kernel (default 0:
+ * off; environment MKPP_TAIL_AFTER).  Once every cell of a launch has been
+ * handed out and no more cells are still on lanes than the warp-cooperative
+ * kernel runs at once, a cell with at least min_attempts attempts is parked
+ * for that kernel, which takes a warp per cell.  The last, slowest cells of a
+ * call then finish faster.  Results do not depend on it: a parked cell ends
+ * bit-identical.  Applies to the 255-register variant. */
+int mkpp_set_tail_parking(int min_attempts);
+
 /* Rate constants of every reaction into ktab[cell + num_cells * reaction].
  * temp/rho/rh/clw/param may be NULL (compile-time environment, 0.5, 0, zeros).
  * status (may be NULL) receives MKPP_CELL_ERR_NON_FINITE_STATE for cells with

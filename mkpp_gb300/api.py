@@ -86,6 +86,7 @@ SIGNATURES = [
     ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_set_cost_order", _i, [_vp, _i]),
+    ("mkpp_set_tail_parking", _i, [_i]),
     ("mkpp_gpu_tangent_workspace_bytes", _sz, [_sz]),
     ("mkpp_gpu_tangent", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_integrate_noalloc", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _vp, _vp, _vp, _vp]),
@@ -290,6 +291,10 @@ class DeviceSolver:
         self._check(self.lib.mkpp_set_launch_tuning(C.c_int(register_variant), C.c_int(blocks_per_sm),
                                                     C.c_int(defer_after)))
         self._ws = None
+
+    def set_tail_parking(self, min_attempts: int):
+        """Park the last cells on lanes after min_attempts attempts (0: off)."""
+        self._check(self.lib.mkpp_set_tail_parking(C.c_int(min_attempts)))
 
     def workspace(self, n: int):
         torch = self.torch

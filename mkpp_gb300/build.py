@@ -44,7 +44,7 @@ def lib_path(mech: str) -> Path:
 # the unrolled attempt of a large mechanism takes one to two minutes of
 # cicc + ptxas per kernel.  The heaviest units come first.
 UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_tangent.cu", "mkpp_capi.cu",
-         "mkpp_plain.cu", "mkpp_persist4.cu", "mkpp_eval.cu", "mkpp_coop.cu", "mkpp_diff.cu")
+         "mkpp_plain.cu", "mkpp_persist4.cu", "mkpp_tail.cu", "mkpp_eval.cu", "mkpp_coop.cu", "mkpp_diff.cu")
 
 
 # Units of a table-driven mechanism (too large to unroll, such as TS1): its

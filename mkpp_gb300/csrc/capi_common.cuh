@@ -56,6 +56,8 @@ inline mkpp::LaunchArgs make_args(size_t cells, double* conc, const double* ktab
 // mkpp_persist4.cu: the 128-register persistent variant.
 int resident_blocks4();
 int launch_persistent4(const mkpp::LaunchArgs& a, double* scratch, int grid, cudaStream_t stream);
+// mkpp_tail.cu: the 255-register persistent variant with tail parking.
+int launch_persistent_tail(const mkpp::LaunchArgs& a, double* scratch, int grid, cudaStream_t stream);
 // mkpp_eval.cu: tendency and dense-Jacobian evaluation.
 int launch_eval_rates(size_t n, const double* conc, const double* ktab, double* out, cudaStream_t stream);
 int launch_eval_jacobian(size_t n, const double* conc, const double* ktab, double* out, cudaStream_t stream);

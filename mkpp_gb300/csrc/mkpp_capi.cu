@@ -111,6 +111,7 @@ struct Tuning {
   int register_variant = 2;
   int blocks_per_sm = 0;
   int defer_after = kDefaultDeferPerStep;
+  int tail_after = 0;  // tail parking threshold in attempts (0: off)
 };
 
 Tuning& tuning() {
@@ -119,6 +120,7 @@ Tuning& tuning() {
     if (const char* e = std::getenv("MKPP_REGISTER_VARIANT")) x.register_variant = std::atoi(e) == 4 ? 4 : 2;
     if (const char* e = std::getenv("MKPP_BLOCKS_PER_SM")) x.blocks_per_sm = std::max(0, std::atoi(e));
     if (const char* e = std::getenv("MKPP_DEFER_AFTER")) x.defer_after = std::max(0, std::atoi(e));
+    if (const char* e = std::getenv("MKPP_TAIL_AFTER")) x.tail_after = std::max(0, std::atoi(e));
     return x;
   }();
   return t;
@@ -167,7 +169,7 @@ const LaunchConfig& launch_config() {
 
 int integrate_grid() { return launch_config().grid; }
 
-// Workspace layout: [queue counter, parked-cell counter | 256 B]
+// Workspace layout: [queue counter, parked-cell counter, active-cell counter | 256 B]
 // [per-block scratch tiles][parked-cell records, one per cell].
 size_t scratch_offset() { return kQueueBytes; }
 size_t defer_offset() {
@@ -198,20 +200,28 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   unsigned char* ws = (unsigned char*)workspace;
   a.queue = (unsigned int*)ws;
   a.defer_count = (unsigned int*)ws + 1;
+  a.active = (unsigned int*)ws + 2;
   double* scratch = StoreInfo::block_bytes ? (double*)(ws + scratch_offset()) : nullptr;
   const LaunchConfig& cfg = launch_config();
-  if (cudaMemsetAsync(ws, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
+  if (cudaMemsetAsync(ws, 0, 3 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
   if (mode == 1) {
-    const long long park = (long long)tuning().defer_after * std::max(1, a.steps);
+    const Tuning& t = tuning();
+    const long long park = (long long)t.defer_after * std::max(1, a.steps);
     a.defer_after = (int)std::min<long long>(park, INT32_MAX);
-    a.defer = a.defer_after > 0 && cfg.coop_ok ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
+    // Tail parking runs in the 255-register variant only.
+    const bool tail = t.tail_after > 0 && cfg.minb == 2;
+    a.defer = (a.defer_after > 0 || tail) && cfg.coop_ok ? (mkpp::Deferred*)(ws + defer_offset()) : nullptr;
     if (!a.defer) a.defer_after = 0;
-    if (cfg.minb == 4) {
+    if (tail && a.defer) {
+      a.tail_after = t.tail_after;
+      a.tail_cells = (unsigned)(cfg.sms * 2 * cfg.coop_warps);
+      if (launch_persistent_tail(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+    } else if (cfg.minb == 4) {
       if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else {
       mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
     }
-    if (a.defer_after > 0) {
+    if (a.defer) {
       if (launch_coop(a, cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream) != MKPP_SUCCESS) {
         return MKPP_ERROR_DEVICE;
       }
@@ -676,6 +686,12 @@ int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions
 // ---- Device-pointer entry points --------------------------------------------
 
 size_t mkpp_gpu_workspace_bytes(size_t num_cells) { return workspace_bytes(num_cells); }
+
+int mkpp_set_tail_parking(int min_attempts) {
+  if (min_attempts < 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  tuning().tail_after = min_attempts;
+  return MKPP_SUCCESS;
+}
 
 int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after) {
   if (register_variant != 0 && register_variant != 2 && register_variant != 4) return MKPP_ERROR_INVALID_ARGUMENT;

@@ -48,6 +48,13 @@ struct LaunchArgs {
   unsigned char* log_acc;
   int* log_n;
   int log_cap;
+  // Tail parking (integrate_persistent_kernel<Mech, MINB, true>): once the
+  // queue is drained and at most tail_cells cells are still on lanes, a cell
+  // with at least tail_after attempts is parked as well.  active counts the
+  // cells on lanes (zeroed before launch).
+  unsigned int* active;
+  int tail_after;
+  unsigned int tail_cells;
 };
 
 // Controller state of a parked cell (see LaunchArgs::defer).
@@ -305,7 +312,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_plain_kernel(LaunchArg
 // so a warp's lanes stay busy even when cells need very different numbers
 // of attempts.  All lanes run the same attempt code on different cells.
 // ---------------------------------------------------------------------------
-template <class Mech, int MINB>
+template <class Mech, int MINB, bool TAIL = false>
 __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
   using Store = typename StoreFor<Mech>::type;
   Store S = make_store<Mech>(scratch, (Store*)nullptr);
@@ -316,9 +323,15 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
   int step = 0, nacc = 0, nrej = 0;
   bool flagged = false;      // cell rejected by the input checks: leave it untouched
   bool capped = false, zero_pivot = false;
+  bool left = false;         // (TAIL) the lane's cell finished or was parked last iteration
   Controller ctl;
   ctl.start(a.dt, a.seed);
   for (;;) {
+    if constexpr (TAIL) {
+      const unsigned gone = __ballot_sync(0xffffffffu, left);
+      if (gone && (int)lane == __ffs(gone) - 1) atomicSub(a.active, (unsigned)__popc(gone));
+      left = false;
+    }
     const bool need = cell < 0;
     const unsigned want = __ballot_sync(0xffffffffu, need);
     if (want) {
@@ -340,6 +353,10 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           }
           ctl.start(a.dt, a.seed);
         }
+      }
+      if constexpr (TAIL) {
+        const unsigned got = __ballot_sync(0xffffffffu, need && cell < (long long)n);
+        if (got && (int)lane == __ffs(got) - 1) atomicAdd(a.active, (unsigned)__popc(got));
       }
     }
     const bool active = cell >= 0 && cell < (long long)n;
@@ -369,8 +386,11 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           } else {
             done = true;
           }
-        } else if (a.defer_after > 0 && nacc + nrej >= a.defer_after) {
-          // Too slow for one lane: park the cell for the cooperative kernel.
+        } else if ((a.defer_after > 0 && nacc + nrej >= a.defer_after) ||
+                   (TAIL && a.tail_after > 0 && nacc + nrej >= a.tail_after && ((nacc + nrej) & 15) == 0 &&
+                    __ldcg(a.queue) >= (unsigned)n && __ldcg(a.active) <= a.tail_cells)) {
+          // Too slow for one lane, or one of the last cells on lanes: park
+          // the cell for the cooperative kernel.
           const unsigned slot = atomicAdd(a.defer_count, 1u);
           Deferred d;
           d.cell = (int)cell;
@@ -384,6 +404,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           a.defer[slot] = d;
           store_state<Mech>(a.conc, (size_t)cell, n, S);
           cell = -1;
+          left = true;
           continue;
         }
       }
@@ -397,6 +418,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         if (a.n_reject) a.n_reject[cc] = nrej;
       }
       cell = -1;
+      left = true;
     }
   }
 }

@@ -58,3 +58,31 @@ def test_cost_order_leaves_results_unchanged(built_libs):
     for a, b in zip(*runs):
         for x, y in zip(a, b):
             assert np.array_equal(x, y, equal_nan=True)
+
+
+@pytest.mark.parametrize("mech", ["small_strato", "saprc99"])
+def test_tail_parking_leaves_results_unchanged(built_libs, mech):
+    """mkpp_set_tail_parking: with 96 cells every cell is handed out at once
+    and fewer cells are on lanes than the cooperative kernel runs, so every
+    cell past 32 attempts is parked at its next multiple of 16 attempts.
+    State, status and attempt counts end bit-identical to the run without
+    tail parking (a window of 2 host steps)."""
+    import torch
+
+    from mkpp_gb300.api import DeviceSolver
+
+    w, s = workloads.make(mech, 96), DeviceSolver(mech)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    outs = []
+    try:
+        for tail in (0, 32):
+            s.set_tail_parking(tail)
+            conc = d(w.conc)
+            st, acc, rej = s.integrate(conc, w.dt, steps=2, temp=d(w.temp), rho=d(w.rho), rh=d(w.rh),
+                                       param=d(w.param), mode="persistent")
+            torch.cuda.synchronize()
+            outs.append((conc.cpu().numpy(), st.cpu().numpy(), acc.cpu().numpy(), rej.cpu().numpy()))
+    finally:
+        s.set_tail_parking(0)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b, equal_nan=True)
