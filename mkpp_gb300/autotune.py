@@ -2,12 +2,14 @@
 
     python -m mkpp_gb300.autotune saprc99 [--cells 65536] [--host-steps 2]
 
-The knobs are those of `mkpp_set_launch_tuning`:
+The knobs are those of `mkpp_set_launch_tuning` and `mkpp_set_tail_parking`:
 * register variant: 2 (up to 255 registers per thread, no spills of the
   unrolled attempt) or 4 (up to 128, twice the resident warps);
 * resident blocks per SM: the register variant's maximum, or fewer;
 * parking threshold: attempts per host step after which the persistent
-  kernel hands a cell to the warp-cooperative kernel (0: never).
+  kernel hands a cell to the warp-cooperative kernel (0: never);
+* tail parking threshold (register variant 2 only): once the queue is drained
+  and few cells remain on lanes, cells past it are handed over too (0: off).
 A block holds 128 cells, one per thread.  The work queue hands out one cell
 per lane (warp-aggregated atomics), so there is no chunk size to tune.
 
@@ -33,15 +35,19 @@ class Candidate:
     register_variant: int
     blocks_per_sm: int          # 0: as many as fit
     defer_after: int            # attempts per host step; 0: never park
+    tail_after: int = 0         # tail parking threshold in attempts; 0: off
 
 
 def candidates() -> list[Candidate]:
     """The search space: both register variants at full and reduced
-    residency, each with parking off, at 1000 and at 3000 attempts."""
+    residency, each with parking off, at 1000 and at 3000 attempts; the
+    full-residency 255-register variant also with tail parking at 300."""
     out = []
     for rv, blocks in ((2, 0), (2, 1), (4, 0), (4, 2)):
         for defer in (0, 1000, 3000):
             out.append(Candidate(rv, blocks, defer))
+            if (rv, blocks) == (2, 0):
+                out.append(Candidate(rv, blocks, defer, 300))
     return out
 
 
@@ -127,6 +133,7 @@ def gpu_measure(mechanism: str, cells: int, host_steps: int):
 
     def measure(c: Candidate) -> float:
         s.set_tuning(c.register_variant, c.blocks_per_sm, c.defer_after)
+        s.set_tail_parking(c.tail_after)
         runs = 1 if c in warmed else 2
         for _ in range(runs):
             conc = conc0.clone()
@@ -157,7 +164,9 @@ def apply(mechanism: str, path: Path | None = None) -> Candidate | None:
 
     c = lookup(mechanism, _current_gpu(), path)
     if c is not None:
-        DeviceSolver(mechanism).set_tuning(c.register_variant, c.blocks_per_sm, c.defer_after)
+        s = DeviceSolver(mechanism)
+        s.set_tuning(c.register_variant, c.blocks_per_sm, c.defer_after)
+        s.set_tail_parking(c.tail_after)
     return c
 
 

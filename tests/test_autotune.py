@@ -15,6 +15,9 @@ def test_candidates_are_valid_and_distinct():
     # Both register budgets, and parking both off and on, are searched.
     assert {c.register_variant for c in cands} == {2, 4}
     assert 0 in {c.defer_after for c in cands} and max(c.defer_after for c in cands) > 0
+    # Tail parking: searched, and only where its kernel exists (255 registers).
+    assert {c.tail_after for c in cands} == {0, 300}
+    assert all(c.register_variant == 2 for c in cands if c.tail_after)
 
 
 def test_search_picks_the_fastest_and_records_failures():
@@ -71,3 +74,15 @@ def test_cache_path_follows_the_environment(tmp_path, monkeypatch):
     monkeypatch.delenv("MKPP_TUNING_CACHE")
     monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
     assert at.cache_path() == tmp_path / "mkpp_gb300" / "tuning.json"
+
+
+def test_cache_entries_without_tail_parking_still_load(tmp_path):
+    """A cache written before tail parking was searched has no tail_after:
+    it reads back with tail parking off."""
+    import json
+
+    path = tmp_path / "tuning.json"
+    gpu = at.gpu_key("NVIDIA GB300", 152)
+    path.write_text(json.dumps({"saprc99": {gpu: {"choice": {"register_variant": 2, "blocks_per_sm": 0,
+                                                            "defer_after": 3000}, "table": []}}}))
+    assert at.lookup("saprc99", gpu, path) == at.Candidate(2, 0, 3000, 0)
