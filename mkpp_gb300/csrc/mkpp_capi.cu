@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "capi_common.cuh"
 
 using namespace mkpp_tu;
@@ -75,6 +77,17 @@ struct mkpp_handle_s {
 };
 
 namespace {
+
+// NVTX range over a scope, named as the reference's Kokkos regions
+// (MKPP_C_API_<mech>: src/mkpp/templates/host_api/mkpp_c_api.cpp.j2:275;
+// MKPP_Dispatch_<mech>: src/mkpp_host/include/mkpp_host/mechanism_manager.hpp:125).
+// Without a profiler attached, NVTX calls do nothing.
+struct NvtxRange {
+  explicit NvtxRange(const std::string& name) { nvtxRangePushA(name.c_str()); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+const std::string kApiRange = std::string("MKPP_C_API_") + Mech::NAME;
+const std::string kDispatchRange = std::string("MKPP_Dispatch_") + Mech::NAME;
 
 int device_fail(mkpp_handle_s* h, cudaError_t err, const char* what) {
   if (h) h->set_error(std::string("FATAL ERROR: ") + what + ": " + cudaGetErrorString(err));
@@ -516,6 +529,7 @@ static int stage_inputs(mkpp_handle_s* h) {
 
 int mkpp_integrate(mkpp_handle_t handle, double dt) {
   if (!handle) return MKPP_ERROR_NULL_POINTER;
+  const NvtxRange range(kApiRange);
   mkpp_handle_s* h = handle;
   if (!h->initialized) {
     h->set_error("FATAL ERROR: MKPP handle must be initialized before integration");
@@ -729,6 +743,7 @@ int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, siz
                          int* accepted, int* rejected, void* workspace, size_t workspace_bytes_, void* stream) {
   const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
   if (rc != MKPP_SUCCESS) return rc;
+  const NvtxRange range(kDispatchRange);
   if (mode != 0 && mode != 1) return MKPP_ERROR_INVALID_ARGUMENT;
   if (k_step_stride != 0 && k_step_stride < num_cells * Mech::NR) return MKPP_ERROR_INVALID_ARGUMENT;
   mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);

@@ -9,7 +9,11 @@ code (csrc/solver.cuh, csrc/mkpp_device.cuh):
 * the emitted per-mechanism code has no while loop: every loop has a
   compile-time trip count or walks a table of known length;
 * every controller loop is bounded by the attempt cap, and no device loop
-  waits on memory another thread writes, so no kernel can spin forever.
+  waits on memory another thread writes, so no kernel can spin forever;
+* every slot a program word addresses (the cooperative stage programs, the
+  table-driven adjoint and the tangent program) lies inside the store the
+  kernel gives that program, checked here from the emitted tables instead
+  of by bounds checks on the device.
 """
 import re
 from pathlib import Path
@@ -69,3 +73,50 @@ def test_no_device_loop_polls_memory(path):
     code = _code(path)
     assert not re.search(r"\bvolatile\b", code)
     assert not re.search(r"atomicCAS\s*\(", code)
+
+
+def _int_const(text, name):
+    """Value of `constexpr int NAME = <literal or A + B>;` in an emitted header."""
+    m = re.search(rf"constexpr int {name} = ([^;]+);", text)
+    assert m, name
+    expr = m.group(1).strip()
+    return sum(int(t) if t.strip().isdigit() else _int_const(text, t.strip()) for t in expr.split("+"))
+
+
+def _words(text, name):
+    m = re.search(rf"const unsigned long long {name}\[(\d+)\] = \{{(.*?)\}};", text, re.S)
+    if not m:
+        return None
+    words = [int(w.strip()[:-3], 0) for w in m.group(2).split(",") if w.strip()]
+    assert len(words) == int(m.group(1))
+    return words
+
+
+def _max_slot(words):
+    from mkpp_gb300.emitter import warp_schedule as ws
+
+    top = -1
+    for w in words:
+        kind, out, a, b, c, _ = ws.decode(w)
+        if kind == 0:
+            continue
+        top = max(top, out) if kind == ws.RCP else max(top, out, a, b, c)
+    return top
+
+
+@pytest.mark.parametrize("path", GENERATED, ids=lambda p: p.name)
+def test_program_slots_lie_inside_their_stores(path):
+    text = path.read_text()
+    coop, adj, tlm = (_int_const(text, n) for n in ("COOP_SLOTS", "NSLOTS_ADJ", "NSLOTS_TLM"))
+    sched = _words(text, "sched")
+    assert sched and _max_slot(sched) < coop
+    adj_prog = _words(text, "adj_prog")
+    assert (adj_prog is not None) == ("TABLE_ATTEMPT = true" in text)
+    if adj_prog is not None:                      # table-driven adjoint
+        assert _max_slot(adj_prog) < adj
+    tlm_prog = _words(text, "tlm_prog")
+    assert tlm_prog and _max_slot(tlm_prog) < tlm
+    assert _int_const(text, "TLM_CB") + _int_const(text, "TLM_NCONST") <= tlm
+    body = text[text.index("static void tlm_step("):]
+    body = body[:body.index("\n  }\n")]
+    assert all(int(i) < tlm for i in re.findall(r"S\[(\d+)\] =", body))
