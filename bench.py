@@ -21,6 +21,7 @@ gpu_launches.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes as C
 import json
 import os
@@ -140,6 +141,21 @@ def barrier(world):
     from mkpp_gb300 import shard
 
     shard.barrier()
+
+
+@contextlib.contextmanager
+def optional_section(result: dict, name: str, guard: bool = True):
+    """A secondary measurement: if it raises (and guard is set), its key in
+    the JSON line records the error instead of the run losing the headline
+    numbers already measured.  Unguarded where ranks must stay in step."""
+    if not guard:
+        yield
+        return
+    try:
+        yield
+    except Exception as e:  # noqa: BLE001
+        result[name] = {"error": f"{type(e).__name__}: {e}"}
+        log(f"{name}: failed: {type(e).__name__}: {e}")
 
 
 def max_over_ranks(x: float, world: int) -> float:
@@ -378,130 +394,135 @@ def main():
     }
 
     if rank == 0 and not args.no_plain:
-        # Forms on a sub-configuration (first forms_cells cells, first
-        # forms_host_steps host steps): plain = one launch per host step, one
-        # thread per cell, no queue; persistent = the window form above.
-        fn, fh = min(n, args.forms_cells), min(hs, args.forms_host_steps)
-        sub = conc0[:, :fn].contiguous()
-        c2 = sub.clone()
-        k2 = ktab[:fh, :, :fn].contiguous()
-        s2, a2, r2 = status[:fn].clone(), acc[:fn].clone(), rej[:fn].clone()
-        res = {}
-        for form in ("plain", "persistent"):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                c2.copy_(sub)
-                s2.zero_()
-                e0.record(stream)
-                if form == "plain":
-                    for s in range(fh):
-                        check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2[s]), C.c_size_t(0), 1,
-                                                       C.c_double(w.dt), C.c_double(seed), args.max_attempts, 0,
-                                                       None, p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
-                              "integrate plain")
-                else:
-                    check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2), C.c_size_t(NR * fn), fh,
-                                                   C.c_double(w.dt), C.c_double(seed), args.max_attempts, 1, None,
-                                                   p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
-                          "integrate persistent")
-                e1.record(stream)
-                stream.synchronize()
-            ms = e0.elapsed_time(e1)
-            res[form] = {"value": fn * fh / (ms * 1e-3), "ms": ms}
-            log(f"form {form}: {ms:.0f} ms")
-        result["forms"] = {"config": f"first {fn} cells x {fh} host steps", "unit": UNIT,
-                           "plain": dict(res["plain"], form="one thread per cell, one launch per host step"),
-                           "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
-                                                                     "one launch for all host steps")}
+        with optional_section(result, "forms", True):
+            # Forms on a sub-configuration (first forms_cells cells, first
+            # forms_host_steps host steps): plain = one launch per host step, one
+            # thread per cell, no queue; persistent = the window form above.
+            fn, fh = min(n, args.forms_cells), min(hs, args.forms_host_steps)
+            sub = conc0[:, :fn].contiguous()
+            c2 = sub.clone()
+            k2 = ktab[:fh, :, :fn].contiguous()
+            s2, a2, r2 = status[:fn].clone(), acc[:fn].clone(), rej[:fn].clone()
+            res = {}
+            for form in ("plain", "persistent"):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    c2.copy_(sub)
+                    s2.zero_()
+                    e0.record(stream)
+                    if form == "plain":
+                        for s in range(fh):
+                            check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2[s]), C.c_size_t(0), 1,
+                                                           C.c_double(w.dt), C.c_double(seed), args.max_attempts, 0,
+                                                           None, p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
+                                  "integrate plain")
+                    else:
+                        check(lib.mkpp_gpu_integrate_k(C.c_size_t(fn), p(c2), p(k2), C.c_size_t(NR * fn), fh,
+                                                       C.c_double(w.dt), C.c_double(seed), args.max_attempts, 1, None,
+                                                       p(s2), p(a2), p(r2), p(ws), C.c_size_t(ws.numel()), sp),
+                              "integrate persistent")
+                    e1.record(stream)
+                    stream.synchronize()
+                ms = e0.elapsed_time(e1)
+                res[form] = {"value": fn * fh / (ms * 1e-3), "ms": ms}
+                log(f"form {form}: {ms:.0f} ms")
+            result["forms"] = {"config": f"first {fn} cells x {fh} host steps", "unit": UNIT,
+                               "plain": dict(res["plain"], form="one thread per cell, one launch per host step"),
+                               "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
+                                                                         "one launch for all host steps")}
 
     if rank == 0 and not args.no_adjoint:
-        # Discrete adjoint (SAPRC99 adjoint configuration): first adjoint_cells
-        # cells, one 3600 s integrate() with checkpoints at accepted steps, loss
-        # sum_c (O3_c - O3t_c)^2 with O3t log-normal (sigma 0.2) around the
-        # forward result; gradients w.r.t. all initial concentrations and all
-        # rate constants.  Reported: adjoint time / checkpointed-forward time.
-        from mkpp_gb300.adjoint import Checkpoints
+        with optional_section(result, "adjoint", True):
+            # Discrete adjoint (SAPRC99 adjoint configuration): first adjoint_cells
+            # cells, one 3600 s integrate() with checkpoints at accepted steps, loss
+            # sum_c (O3_c - O3t_c)^2 with O3t log-normal (sigma 0.2) around the
+            # forward result; gradients w.r.t. all initial concentrations and all
+            # rate constants.  Reported: adjoint time / checkpointed-forward time.
+            from mkpp_gb300.adjoint import Checkpoints
 
-        cap = 1536
-        # Checkpoints hold cap x NV doubles per cell: at most 100 GB of them
-        # (SAPRC99: 65536 cells = 63 GB; TS1 would need 168 GB for 65536).
-        na = min(n, args.adjoint_cells, int(100e9 // (cap * plan.n_var * 8)))
-        ca0 = conc0[:, :na].contiguous()
-        ka = ktab[0, :, :na].contiguous()
-        del ktab
-        torch.cuda.empty_cache()
-        ck = Checkpoints(w.mechanism, na, cap, dev)
-        ev_f = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        ev_a = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        ca = ca0.clone()
-        with torch.cuda.stream(stream):
-            ev_f[0].record(stream)
-            ck.forward(ca, ka, 3600.0, seed, args.max_attempts)
-            ev_f[1].record(stream)
-            stream.synchronize()
-            o3 = raw["species"].index("O3")
-            rng = torch.Generator(device="cpu").manual_seed(2718)
-            target = ca[o3] * torch.exp(0.2 * torch.randn(na, generator=rng, dtype=f64)).to(dev)
-            lam = torch.zeros_like(ca)
-            lam[o3] = 2.0 * (ca[o3] - target)
-            ev_a[0].record(stream)
-            gc, gk = ck.adjoint(ka, lam)
-            ev_a[1].record(stream)
-            stream.synchronize()
-        fms, ams = ev_f[0].elapsed_time(ev_f[1]), ev_a[0].elapsed_time(ev_a[1])
-        cnt = ck.count.cpu().numpy()
-        sts = ck.status.cpu().numpy()
-        result["adjoint"] = {
-            "config": f"first {na} cells, one 3600 s integrate(), loss sum (O3 - O3t)^2, O3t log-normal sigma 0.2",
-            "forward_checkpointed_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
-            "accepted_steps_pct": {q: float(np.percentile(cnt, q)) for q in (50, 99, 100)},
-            "checkpoint_cap": cap, "cell_status_counts": np.bincount(sts, minlength=6).tolist(),
-            "gradients": f"dL/dC0 for all species (fixed species 0) and dL/dk for all {len(raw['reactions'])} "
-                         "reactions, FP64",
-            "finite_gradients_frac": float(torch.isfinite(gc).all(0).double().mean()),
-        }
-        log(f"adjoint: forward {fms:.0f} ms, adjoint {ams:.0f} ms, ratio {ams / fms:.2f}")
-        del ck, gc, gk
-        torch.cuda.empty_cache()
+            cap = 1536
+            # Checkpoints hold cap x NV doubles per cell: at most 100 GB of them
+            # (SAPRC99: 65536 cells = 63 GB; TS1 would need 168 GB for 65536).
+            na = min(n, args.adjoint_cells, int(100e9 // (cap * plan.n_var * 8)))
+            ca0 = conc0[:, :na].contiguous()
+            ka = ktab[0, :, :na].contiguous()
+            del ktab
+            torch.cuda.empty_cache()
+            ck = Checkpoints(w.mechanism, na, cap, dev)
+            ev_f = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev_a = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ca = ca0.clone()
+            with torch.cuda.stream(stream):
+                ev_f[0].record(stream)
+                ck.forward(ca, ka, 3600.0, seed, args.max_attempts)
+                ev_f[1].record(stream)
+                stream.synchronize()
+                o3 = raw["species"].index("O3")
+                rng = torch.Generator(device="cpu").manual_seed(2718)
+                target = ca[o3] * torch.exp(0.2 * torch.randn(na, generator=rng, dtype=f64)).to(dev)
+                lam = torch.zeros_like(ca)
+                lam[o3] = 2.0 * (ca[o3] - target)
+                ev_a[0].record(stream)
+                gc, gk = ck.adjoint(ka, lam)
+                ev_a[1].record(stream)
+                stream.synchronize()
+            fms, ams = ev_f[0].elapsed_time(ev_f[1]), ev_a[0].elapsed_time(ev_a[1])
+            cnt = ck.count.cpu().numpy()
+            sts = ck.status.cpu().numpy()
+            result["adjoint"] = {
+                "config": f"first {na} cells, one 3600 s integrate(), loss sum (O3 - O3t)^2, O3t log-normal sigma 0.2",
+                "forward_checkpointed_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
+                "accepted_steps_pct": {q: float(np.percentile(cnt, q)) for q in (50, 99, 100)},
+                "checkpoint_cap": cap, "cell_status_counts": np.bincount(sts, minlength=6).tolist(),
+                "gradients": f"dL/dC0 for all species (fixed species 0) and dL/dk for all {len(raw['reactions'])} "
+                             "reactions, FP64",
+                "finite_gradients_frac": float(torch.isfinite(gc).all(0).double().mean()),
+            }
+            log(f"adjoint: forward {fms:.0f} ms, adjoint {ams:.0f} ms, ratio {ams / fms:.2f}")
+            del ck, gc, gk
+            torch.cuda.empty_cache()
 
     if not args.no_e2e:
-        # End to end through the reference-facing host C ABI with pinned host buffers.
-        host_conc = torch.from_numpy(w.conc).pin_memory()
-        work_conc = host_conc.clone().pin_memory()
-        host_par = [torch.from_numpy(w.param_at(s)).pin_memory() for s in range(hs)]
-        t_h, r_h, p_h = (torch.from_numpy(a).pin_memory() for a in (w.temp, w.rho, w.pressure))
-        rh_h = torch.from_numpy(w.rh).pin_memory()
-        ctx = MechanismContext(w.mechanism, n)
-        conc_np, par_np = work_conc.numpy(), [x.numpy() for x in host_par]
-        ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
-        ctx.set_aerosol(relative_humidity=rh_h.numpy())
-        if args.e2e_cost_order:
-            ctx.set_cost_order(True)
-        e2e_times = []
-        for rep in range(1):
-            work_conc.copy_(host_conc)
-            barrier(world)
-            t0 = time.perf_counter()
-            for s in range(hs):
-                ctx.set_rate_parameters(par_np[s])
-                ctx.integrate(w.dt)
-            e2e_times.append(time.perf_counter() - t0)
-        e2e_s = max_over_ranks(min(e2e_times), world)
-        log(f"e2e: {e2e_s:.1f} s")
-        h2d = hs * n * 8 * (NS + 3 + NP)
-        d2h = hs * n * 8 * NS
-        result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                         "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24",
-                         "cost_order": bool(args.e2e_cost_order)}
-        ctx.close()
+        with optional_section(result, "e2e", world == 1):
+            # End to end through the reference-facing host C ABI with pinned host buffers.
+            host_conc = torch.from_numpy(w.conc).pin_memory()
+            work_conc = host_conc.clone().pin_memory()
+            host_par = [torch.from_numpy(w.param_at(s)).pin_memory() for s in range(hs)]
+            t_h, r_h, p_h = (torch.from_numpy(a).pin_memory() for a in (w.temp, w.rho, w.pressure))
+            rh_h = torch.from_numpy(w.rh).pin_memory()
+            ctx = MechanismContext(w.mechanism, n)
+            conc_np, par_np = work_conc.numpy(), [x.numpy() for x in host_par]
+            ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
+            ctx.set_aerosol(relative_humidity=rh_h.numpy())
+            if args.e2e_cost_order:
+                ctx.set_cost_order(True)
+            e2e_times = []
+            for rep in range(1):
+                work_conc.copy_(host_conc)
+                barrier(world)
+                t0 = time.perf_counter()
+                for s in range(hs):
+                    ctx.set_rate_parameters(par_np[s])
+                    ctx.integrate(w.dt)
+                e2e_times.append(time.perf_counter() - t0)
+            e2e_s = max_over_ranks(min(e2e_times), world)
+            log(f"e2e: {e2e_s:.1f} s")
+            h2d = hs * n * 8 * (NS + 3 + NP)
+            d2h = hs * n * 8 * NS
+            result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                             "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24",
+                             "cost_order": bool(args.e2e_cost_order)}
+            ctx.close()
 
     if rank == 0 and world == 1:
-        threads = os.cpu_count() or 1
-        kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
-        log(f"cpu baseline ({kind}): {el:.1f} s")
-        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                                  "sample": f"first {args.cpu_cells} of {n} cells x {hs} host steps of {w.dt:g} s",
-                                  "seconds": el}
+        with optional_section(result, "cpu_baseline", True):
+            threads = os.cpu_count() or 1
+            kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
+            log(f"cpu baseline ({kind}): {el:.1f} s")
+            result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                                      "sample": f"first {args.cpu_cells} of {n} cells x {hs} host steps of {w.dt:g} s",
+                                      "seconds": el}
+
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:
