@@ -20,6 +20,9 @@ small JSON fixtures, so the tests never need the reference at run time:
   two 300 s segments with photolysis slots scaled by 1.0 and 1.05, T and air
   density (runners/mkpp/main.cpp:212-215, 333-344), and the tolerances of
   the shipped generated solver (mkpp-generated/ts1.hpp);
+* fortran_bindings.json  the C functions the reference's Fortran module binds
+  (src/mkpp/templates/host_api/mkpp_mod.f90.j2, its bind(C) interfaces): name
+  and, per argument, how it crosses the ABI (pointer, size_t, int, double);
 * ts1_reference_rates.json  F and the nonzero dense Jacobian entries of the
   reference's own generated TS1 solver (compute_rates / compute_jacobian,
   regenerated and compiled by oracle/ref_build.py) at the inputs above,
@@ -66,13 +69,39 @@ def lu_tables(ref: Path):
         (HERE / f"lu_tables_{mech}.json").write_text(json.dumps(out, separators=(",", ":")))
 
 
+def fortran_bindings(ref: Path):
+    """The bind(C) interfaces of the Fortran module template, as ABI classes:
+    an argument with the VALUE attribute passes its kind by value, any other
+    (intent(out) scalars, c_ptr by reference, character arrays) a pointer."""
+    text = (ref / "src/mkpp/templates/host_api/mkpp_mod.f90.j2").read_text()
+    kinds = {"c_ptr": "ptr", "c_size_t": "size_t", "c_int": "int", "c_double": "double"}
+    out = []
+    for m in re.finditer(r'function (\w+)\(([^)]*)\) bind\(C, name="(\w+)"\)(.*?)end function', text, re.S):
+        args = [a.strip() for a in m.group(2).split(",") if a.strip()]
+        decl = {}
+        for line in m.group(4).splitlines():
+            km = re.match(r"\s*(type|integer|real|character)\((?:kind=)?(\w+)\)(.*?)::(.*)", line)
+            if not km:
+                continue
+            names = [n.strip().split("(")[0] for n in km.group(4).split(",")]
+            by_value = "value" in km.group(3)
+            cls = kinds.get(km.group(2), "ptr") if by_value else "ptr"
+            for n in names:
+                decl[n] = cls
+        out.append({"name": m.group(3), "args": [decl[a] for a in args], "returns": "int"})
+    (HERE / "fortran_bindings.json").write_text(json.dumps(
+        {"source": "src/mkpp/templates/host_api/mkpp_mod.f90.j2", "functions": out}, indent=1))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
-    ap.add_argument("--lu-only", action="store_true", help="write the lu_tables_<mech>.json fixtures only")
+    ap.add_argument("--lu-only", action="store_true",
+                    help="write the lu_tables_<mech>.json and fortran_bindings.json fixtures only")
     args = ap.parse_args()
     ref = Path(args.reference)
     lu_tables(ref)
+    fortran_bindings(ref)
     if args.lu_only:
         return
     run = json.loads((ref / "reports/native-kokkos-5.1.1/final-mkpp-chapman.stdout.json").read_text())

@@ -43,3 +43,40 @@ def test_library_exports_every_declared_symbol(mech):
     from mkpp_gb300 import api
 
     api.load_library(mech)
+
+
+def _c_signatures():
+    """{name: (return class, [argument classes])} from include/mkpp.h: a
+    pointer (or the mkpp_handle_t pointer typedef) is "ptr", else the type."""
+    text = (ROOT / "include" / "mkpp.h").read_text()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*(int|size_t)\s+(mkpp_\w+)\s*\(([^)]*)\)\s*;", text, re.M):
+        args = []
+        for a in (x.strip() for x in m.group(3).split(",")):
+            if not a or a == "void":
+                continue
+            if "*" in a or a.split()[0] == "mkpp_handle_t":
+                args.append("ptr")
+            else:
+                args.append(" ".join(a.replace("const ", "").split()[:-1]))
+        out[m.group(2)] = (m.group(1), args)
+    return out
+
+
+def test_reference_fortran_module_binds_the_header():
+    """The reference's Fortran module (src/mkpp/templates/host_api/
+    mkpp_mod.f90.j2) binds 17 C functions with bind(C); every one exists in
+    include/mkpp.h with the same argument count and ABI classes (pointer,
+    size_t, int, double) and an int result, so the unchanged module links
+    against these libraries.  The interfaces come from the committed fixture
+    tests/golden/fortran_bindings.json (tests/golden/make_golden.py)."""
+    import json
+
+    fixture = json.loads((ROOT / "tests" / "golden" / "fortran_bindings.json").read_text())
+    c = _c_signatures()
+    assert len(fixture["functions"]) == 17
+    for f in fixture["functions"]:
+        assert f["name"] in c, f["name"]
+        ret, args = c[f["name"]]
+        assert ret == f["returns"] and args == f["args"], (f["name"], args, f["args"])
