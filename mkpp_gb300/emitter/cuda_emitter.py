@@ -1438,13 +1438,44 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
     return text.replace("struct Mech {", plan._coop_tables + "\nstruct Mech {", 1)
 
 
-def write(name: str, out_dir: Path = GEN_DIR) -> Path:
-    plan = load(name)
-    out_dir.mkdir(parents=True, exist_ok=True)
-    path = out_dir / f"{name}.cuh"
-    text = emit_mechanism(plan)
+def emit_host_header(plan) -> str:
+    """generated/host_api/<m>/mkpp.h: the C ABI (include/mkpp.h) plus the
+    mechanism's sizes, the per-mechanism constants of the reference's
+    generated header (src/mkpp/templates/host_api/mkpp.h.j2:29-33)."""
+    raw = plan.raw
+    guard = f"MKPP_GB300_{plan.name.upper()}_MKPP_H"
+    return f"""/*
+ * mkpp.h of the {plan.name} library (libmkpp_{plan.name}.so), generated from its plan.
+ * The C ABI of include/mkpp.h plus the mechanism's sizes, as the header the
+ * reference generates per mechanism defines them
+ * (src/mkpp/templates/host_api/mkpp.h.j2:29-33).  A host model built against
+ * that header puts this directory on its include path instead.
+ */
+#ifndef {guard}
+#define {guard}
+
+#include "../../../../include/mkpp.h"
+
+#define MKPP_NUM_RATE_PARAMETERS {raw["num_rate_parameters"]}
+#define MKPP_NUM_SPECIES   {len(raw["species"])}
+#define MKPP_NUM_REACTIONS {raw["num_reactions"]}
+#define MKPP_NUM_PHOTOLYSIS {raw["num_photolysis"]}
+
+#endif
+"""
+
+
+def _write_if_changed(path: Path, text: str) -> None:
+    path.parent.mkdir(parents=True, exist_ok=True)
     if not path.exists() or path.read_text() != text:
         path.write_text(text)
+
+
+def write(name: str, out_dir: Path = GEN_DIR) -> Path:
+    plan = load(name)
+    path = out_dir / f"{name}.cuh"
+    _write_if_changed(path, emit_mechanism(plan))
+    _write_if_changed(out_dir / "host_api" / name / "mkpp.h", emit_host_header(plan))
     return path
 
 

@@ -17,9 +17,14 @@ with MKPP_ERROR_DEVICE (-107) and the CUDA runtime's reason (there is no CPU
 fallback); on a GB300 it succeeds.
 """
 import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
 
 import numpy as np
 import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
 
 MECH = "chapman"
 
@@ -131,3 +136,26 @@ def test_compute_without_a_gpu_fails_loudly(lib):
             assert np.all(conc == 1e9)
     finally:
         assert lib.mkpp_destroy_handle(h) == 0
+
+
+@pytest.mark.parametrize("mech", ["chapman", "ts1"])
+def test_reference_contract_program_against_generated_header(mech, tmp_path):
+    """tests/capi/c_abi_contract.c, the reference's test_c_abi.cpp cases
+    written in C11, compiled with gcc against the mechanism's generated
+    mkpp.h (mkpp_gb300/generated/host_api/<m>/, which adds MKPP_NUM_SPECIES
+    and the other sizes to include/mkpp.h) and linked to its library."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    from mkpp_gb300 import build
+
+    try:
+        lib = build.build((mech,))[0]
+    except RuntimeError as e:  # no nvcc
+        pytest.skip(str(e))
+    exe = tmp_path / "c_abi_contract"
+    inc = ROOT / "mkpp_gb300" / "generated" / "host_api" / mech
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{inc}",
+                    str(ROOT / "tests" / "capi" / "c_abi_contract.c"), str(lib),
+                    f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stderr

@@ -65,6 +65,8 @@ def test_generated_header_is_current(mech):
     text = cuda_emitter.emit_mechanism(plan)
     path = cuda_emitter.GEN_DIR / f"{mech}.cuh"
     assert path.read_text() == text, "regenerate with python -m mkpp_gb300.emitter.cuda_emitter"
+    host = cuda_emitter.GEN_DIR / "host_api" / mech / "mkpp.h"
+    assert host.read_text() == cuda_emitter.emit_host_header(plan)
 
 
 def test_tableaux_match_reference_coefficients():
