@@ -59,10 +59,12 @@ def _yaml_stub():
     sys.modules["yaml"] = m
 
 
-def generate(mech: str, reference: str = DEFAULT_REFERENCE) -> Path:
-    """Step 1: the reference compiler writes gen/<mech>/<mech>.hpp and fragments."""
-    out = GEN / mech
-    if (out / f"{mech}.hpp").exists():
+def generate(mech: str, reference: str = DEFAULT_REFERENCE, host_api: bool = False) -> Path:
+    """Step 1: the reference compiler writes gen/<mech>/<mech>.hpp and fragments
+    (host_api: host_api/<mech>/ with its generated host API as well: mkpp.h,
+    the C++ wrapper mkpp.hpp, the C ABI and the Fortran module)."""
+    out = (REF / "host_api" / mech) if host_api else (GEN / mech)
+    if (out / ("mkpp.hpp" if host_api else f"{mech}.hpp")).exists():
         return out
     out.mkdir(parents=True, exist_ok=True)
     env = out / "env.json"
@@ -84,7 +86,7 @@ def generate(mech: str, reference: str = DEFAULT_REFERENCE) -> Path:
         "mech.metadata['rtol'] = [env.solver_rtol] * len(mech.species); "
         "b = partition_reactions(mech); mech.partition_metadata = b.get('metadata'); "
         "prepare_adjoint_and_tlm(mech); mech.sympy_metadata = prepare_unified_jacobian(mech); "
-        f"generate_headers(mech, out_dir={str(out)!r}, solver_name='ros3')"
+        f"generate_headers(mech, out_dir={str(out)!r}, solver_name='ros3', generate_host_api={host_api!r})"
     )
     subprocess.run([sys.executable, "-c", code], check=True, cwd=str(out),
                    env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"))

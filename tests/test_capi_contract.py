@@ -159,3 +159,38 @@ def test_reference_contract_program_against_generated_header(mech, tmp_path):
                     f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0 and out.stdout.strip() == "ok", out.stderr
+
+
+@pytest.mark.parametrize("mech", ["chapman", "ts1"])
+def test_reference_cpp_wrapper_and_sizes(mech, tmp_path):
+    """The reference's own generated host API for the mechanism (generated
+    here by its compiler, oracle/ref_build.py; skipped where the reference
+    is absent): its mkpp.h defines the same MKPP_NUM_* sizes as this
+    repository's generated host_api/<m>/mkpp.h, and its C++ wrapper mkpp.hpp,
+    unchanged, compiles against this repository's header and drives the
+    library (tests/capi/cpp_wrapper_check.cpp)."""
+    import re
+
+    from oracle import ref_build
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    try:
+        gen = ref_build.generate(mech, host_api=True)
+    except Exception as e:  # noqa: BLE001
+        pytest.skip(f"reference host API not generated: {e}")
+    if not (gen / "mkpp.hpp").exists():
+        pytest.skip("reference host API not generated")
+    from mkpp_gb300 import build
+
+    lib = build.build((mech,))[0]
+    ours = ROOT / "mkpp_gb300" / "generated" / "host_api" / mech
+    sizes = lambda t: dict(re.findall(r"#define (MKPP_NUM_\w+)\s+(\d+)", t))  # noqa: E731
+    assert sizes((ours / "mkpp.h").read_text()) == sizes((gen / "mkpp.h").read_text())
+    (tmp_path / "mkpp.hpp").write_text((gen / "mkpp.hpp").read_text())
+    exe = tmp_path / "cpp_wrapper_check"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", f"-I{ours}", f"-I{tmp_path}",
+                    str(ROOT / "tests" / "capi" / "cpp_wrapper_check.cpp"), str(lib),
+                    f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", (out.returncode, out.stderr)
