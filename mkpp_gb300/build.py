@@ -48,8 +48,8 @@ UNITS = ("mkpp_adjoint.cu", "mkpp_checkpoint.cu", "mkpp_replay.cu", "mkpp_tangen
 
 
 # Units of a table-driven mechanism (too large to unroll, such as TS1): its
-# unrolled F/J evaluation kernels would take minutes to compile, so the
-# evaluation entries are stubs.
+# unrolled F/J evaluation kernels would take minutes to compile, so its
+# evaluation entries walk a table instead (mkpp_eval_table.cu).
 UNROLLED_ONLY = ("mkpp_eval.cu",)
 
 
@@ -61,12 +61,12 @@ def is_table(mech: str) -> bool:
 
 def units(mech: str) -> tuple[str, ...]:
     if is_table(mech):
-        return tuple(u for u in UNITS if u not in UNROLLED_ONLY) + ("mkpp_eval_stub.cu",)
+        return tuple(u for u in UNITS if u not in UNROLLED_ONLY) + ("mkpp_eval_table.cu",)
     return UNITS
 
 
 def _sources(mech: str) -> list[Path]:
-    return [*(CSRC / u for u in units(mech)), CSRC / "capi_common.cuh", CSRC / "solver.cuh",
+    return [*(CSRC / u for u in units(mech)), CSRC / "capi_common.cuh", CSRC / "solver.cuh", CSRC / "eval_common.cuh",
             CSRC / "mkpp_device.cuh", GEN / f"{mech}.cuh", INCLUDE / "mkpp.h", Path(__file__)]
 
 

@@ -501,14 +501,6 @@ static int ensure_device(mkpp_handle_s* h, size_t out_bytes) {
   return MKPP_SUCCESS;
 }
 
-// Rate and Jacobian evaluation are unrolled code, which a table-driven
-// mechanism (one too large to unroll) does not have.
-static int table_unavailable(mkpp_handle_s* h, const char* what) {
-  h->set_error(std::string("FATAL ERROR: ") + what + " evaluation is not available for the table-driven mechanism " +
-               Mech::NAME);
-  return MKPP_ERROR_INVALID_STATE;
-}
-
 // Copy the bound host inputs to the device and compute the rate constants.
 static int stage_inputs(mkpp_handle_s* h) {
   DeviceBuffers& d = h->dev;
@@ -596,7 +588,6 @@ int mkpp_evaluate_rates(mkpp_handle_t handle, double* rates_out) {
   const size_t bytes = n * Mech::NS * sizeof(double);
   int rc = ensure_device(h, bytes);
   if (rc != MKPP_SUCCESS) return rc;
-  if (Mech::TABLE_ATTEMPT) return table_unavailable(h, "rate");
   rc = stage_inputs(h);
   if (rc != MKPP_SUCCESS) return rc;
   if (launch_eval_rates(n, h->dev.conc, h->dev.ktab, h->dev.out, h->stream) != MKPP_SUCCESS)
@@ -623,7 +614,6 @@ int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out) {
   const size_t bytes = n * Mech::NS * Mech::NS * sizeof(double);
   int rc = ensure_device(h, bytes);
   if (rc != MKPP_SUCCESS) return rc;
-  if (Mech::TABLE_ATTEMPT) return table_unavailable(h, "Jacobian");
   rc = stage_inputs(h);
   if (rc != MKPP_SUCCESS) return rc;
   if (launch_eval_jacobian(n, h->dev.conc, h->dev.ktab, h->dev.out, h->stream) != MKPP_SUCCESS)

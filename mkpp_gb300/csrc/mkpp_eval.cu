@@ -1,18 +1,12 @@
 // Tendency and dense-Jacobian evaluation of one mechanism library
 // (compute_rates / compute_jacobian of the reference,
 // src/mkpp/templates/kernel_functions/compute_{rates,jacobian}.j2).
-#include "capi_common.cuh"
+#include "eval_common.cuh"
 
 using namespace mkpp_tu;
+using mkpp_eval::CellState;
 
 namespace {
-
-// State accessor over a cell's row of the (species x cells) array.
-struct CellState {
-  const double* conc;
-  size_t c, n;
-  __device__ __forceinline__ double operator()(int i) const { return conc[c + n * Mech::var_phys(i)]; }
-};
 
 __global__ void __launch_bounds__(128, 1) eval_rates_kernel(size_t n, const double* conc, const double* ktab,
                                                          double* out) {
@@ -45,29 +39,6 @@ __global__ void __launch_bounds__(128, 1) eval_jacobian_kernel(size_t n, const d
   Mech::for_each_w_slot([&](int slot, int, int) { S[slot] = -S[slot]; });
 }
 
-__global__ void __launch_bounds__(128, 1) mkpp_fixed_columns_kernel(size_t n, const double* conc, const double* temp,
-                                                                 const double* rho, const double* rh,
-                                                                 const double* clw, const double* param,
-                                                                 double* out) {
-  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const CellState y{conc, c, n};
-  const double T = (Mech::RUNTIME_ENV && temp) ? temp[c] : Mech::ENV_T;
-  const double RHO = (Mech::RUNTIME_ENV && rho) ? rho[c] : Mech::ENV_RHO;
-  const double RH = rh ? rh[c] : 0.5;
-  const double CLW = clw ? clw[c] : 0.0;
-  const mkpp::CellRow fix{conc + c, n};
-  const size_t NS = Mech::NS;
-  auto put = [&](int row, int col, double v) { out[c + n * (row + NS * col)] = v; };
-  if (param) {
-    const mkpp::CellRow P{param + c, n};
-    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
-  } else {
-    const mkpp::ZeroRow P;
-    Mech::jac_fixed_columns(P, fix, T, RHO, RH, CLW, y, put);
-  }
-}
-
 }  // namespace
 
 namespace mkpp_tu {
@@ -84,8 +55,7 @@ int launch_eval_jacobian(size_t n, const double* conc, const double* ktab, doubl
 
 int launch_fixed_columns(size_t n, const double* conc, const double* temp, const double* rho, const double* rh,
                          const double* clw, const double* param, double* out, cudaStream_t stream) {
-  mkpp_fixed_columns_kernel<<<launch_grid(n, 128), 128, 0, stream>>>(n, conc, temp, rho, rh, clw, param, out);
-  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+  return mkpp_eval::launch_fixed_columns_kernel(n, conc, temp, rho, rh, clw, param, out, stream);
 }
 
 }  // namespace mkpp_tu

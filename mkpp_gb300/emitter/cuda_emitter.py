@@ -283,16 +283,24 @@ def _coop_build(plan, nv, stages, A, C, NewF, K0, Y, FS, DY, nslots, table=False
         P.solve(plan, kb)
         progs.append(P.ops)
     sched = [warp_schedule.schedule(ops) for ops in progs]
-    adj_ops = None
+    adj_ops = eval_ops = None
     if table:
         P = program()
         _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, Mech_KT, adj, cterm_slot)
         adj_ops = P.ops
+        # The evaluation entries: W with 1/(gamma h) = 0 (that is -J on the W
+        # slots) and F(y) into S[FS..], the first stage's code without the LU.
+        P = program()
+        jac_w(P)
+        fun(P, Y)
+        eval_ops = P.ops
+        assert all(op[0] != warp_schedule.RCP for op in eval_ops)
     nconst = 4 + len(cterm_slot) + len(literals)
     const_vals = ["-0.0", "0.0", "1.0", "0.0"] + ["0.0"] * len(cterm_slot) + [_lit(v) for v in literals]
     return {"progs": progs, "sched": sched, "npart": npart, "nq": nq, "Q": Q, "D": D, "CB": CB,
             "nconst": nconst, "const_vals": const_vals, "literals": literals, "cterm_slot": cterm_slot,
-            "KT": Mech_KT, "total": CB + nconst, "adj": adj, "adj_ops": adj_ops, "A": A, "NewF": NewF}
+            "KT": Mech_KT, "total": CB + nconst, "adj": adj, "adj_ops": adj_ops, "eval_ops": eval_ops,
+            "A": A, "NewF": NewF}
 
 
 def _adjoint_program(plan, P, nv, stages, A, C, M, NewF, K0, Y, KT, adj, cterm_slot):
@@ -657,6 +665,24 @@ def _emit_table_adjoint(c, coop):
     c("      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
     c("    }")
     c("  }")
+    c("")
+    c("  // ---- tendencies and Jacobian (table-driven evaluation entries) ----")
+    c("  // For y in S[Y..]: F(y) into S[F..] and W with 1/(gamma h) = 0, that is")
+    c("  // -J, into the W slots of the LU store.  Walks coop::eval_prog, the")
+    c("  // first stage's partials, W and F code without the factorization.")
+    c("  template <class SA, class KA>")
+    c("  __device__ __forceinline__ static void eval_step(SA& S, const KA& k) {")
+    c("    for (int r = 0; r < NR; ++r) S[KT + r] = k(r);")
+    c("    for (int i = 0; i < NCONST; ++i) S[CB + i] = coop::const_val[i];")
+    c("    S[CB + 3] = 0.0;  // 1/(gamma h)")
+    c("    for (int n = 0; n < coop::EVAL_OPS; ++n) {")
+    c("      const unsigned long long w = __ldg(coop::eval_prog + n);")
+    c("      const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);")
+    c("      const double a = __longlong_as_double(__double_as_longlong(S[(lo >> 16) & 0x7fffu]) ^")
+    c("                                            ((long long)(lo >> 31) << 63));")
+    c("      S[lo & 0xffffu] = fma(a, S[hi & 0xffffu], S[(hi >> 16) & 0x7fffu]);")
+    c("    }")
+    c("  }")
 
 
 def _emit_table_attempt_head(c, coop, C):
@@ -732,6 +758,10 @@ def _emit_coop(c, plan, coop, nv, ns, stages, C, M, E, K0, Y, FS, DY):
         ops = coop["adj_ops"]
         t(f"constexpr int ADJ_OPS = {len(ops)};")
         _c_u64_array(t, "adj_prog", warp_schedule.encode(ops, [[i] for i in range(len(ops))], lanes=1))
+    if coop["eval_ops"] is not None:
+        ops = coop["eval_ops"]
+        t(f"constexpr int EVAL_OPS = {len(ops)};")
+        _c_u64_array(t, "eval_prog", warp_schedule.encode(ops, [[i] for i in range(len(ops))], lanes=1))
     tlm = _tlm_build(plan, nv, stages, coop["A"], C, M, coop["NewF"], K0, Y, Mech_KT, coop["total"])
     tlm_code = _Code()
     _emit_tlm(tlm_code, t, tlm, C)

@@ -2,6 +2,8 @@
 // one step, of an emitted mechanism header on the host (TEST INFRASTRUCTURE
 // ONLY).  The store is a plain array of the per-cell slots (the layout of
 // Mech: Y, stage vectors K0.., F, DY, KT), the rate constants a plain array.
+#include <vector>
+
 #include MKPP_MECH_HEADER
 
 namespace {
@@ -29,13 +31,29 @@ struct RowOut {
 
 // Tendencies F[s] and the dense Jacobian J[row + NS * col] of one cell from
 // the emitted fun(), jac_w() (with 1/(gamma h) = 0, negated) and
-// jac_fixed_columns(), composed as the evaluation kernels compose them.
-// A table-driven mechanism has none of the three: returns -1.
+// jac_fixed_columns(), composed as the evaluation kernels compose them; for
+// a table-driven mechanism from eval_step() on a slot store instead of the
+// first two.
 template <class M>
 int evaluate(const double* conc, const double* param, double T, double RHO, double RH, double CLW,
              const double* k, double* F, double* J) {
   if constexpr (M::TABLE_ATTEMPT) {
-    return -1;
+    const int NS = M::NS;
+    std::vector<double> slots(M::NSLOTS, 0.0);
+    Store S{slots.data()};
+    for (int i = 0; i < M::NV; ++i) S[M::Y + i] = conc[M::var_phys(i)];
+    M::eval_step(S, Rates{k});
+    for (int s = 0; s < NS; ++s) F[s] = 0.0;
+    for (int e = 0; e < NS * NS; ++e) J[e] = 0.0;
+    for (int i = 0; i < M::NV; ++i) F[M::var_phys(i)] = S[M::F + i];
+    M::for_each_w_slot([&](int slot, int, int) { J[M::lu_prow(slot) + NS * M::lu_pcol(slot)] = -S[slot]; });
+    struct Y {
+      const double* c;
+      double operator()(int i) const { return c[M::var_phys(i)]; }
+    } y{conc};
+    M::jac_fixed_columns(Row{param}, Row{conc}, T, RHO, RH, CLW, y,
+                         [&](int row, int col, double v) { J[row + NS * col] = v; });
+    return 0;
   } else {
     const int NS = M::NS;
     struct Y {
@@ -69,8 +87,7 @@ void hostsim_rate_constants(const double* conc, const double* param, double T, d
   Mech::rate_constants(Row{param}, Row{conc}, T, RHO, RH, CLW, out);
 }
 
-// Tendencies and dense Jacobian of one cell (evaluate() above); -1 for a
-// table-driven mechanism.
+// Tendencies and dense Jacobian of one cell (evaluate() above).
 int hostsim_evaluate(const double* conc, const double* param, double T, double RHO, double RH, double CLW,
                      const double* k, double* F, double* J) {
   return evaluate<Mech>(conc, param, T, RHO, RH, CLW, k, F, J);

@@ -25,8 +25,8 @@ def test_header_declares_reference_entry_points():
 
 @pytest.mark.parametrize("mech", ["chapman", "ts1"])
 def test_library_exports_every_declared_symbol(mech):
-    """Unrolled (chapman) and table-driven (ts1, whose evaluation entries
-    are stubs) libraries export the whole C ABI."""
+    """Unrolled (chapman) and table-driven (ts1) libraries export the whole
+    C ABI."""
     from mkpp_gb300 import build
     from mkpp_gb300.api import SIGNATURES
 

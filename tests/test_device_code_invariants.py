@@ -11,7 +11,7 @@ code (csrc/solver.cuh, csrc/mkpp_device.cuh):
 * every controller loop is bounded by the attempt cap, and no device loop
   waits on memory another thread writes, so no kernel can spin forever;
 * every slot a program word addresses (the cooperative stage programs, the
-  table-driven adjoint and the tangent program) lies inside the store the
+  table-driven adjoint and evaluation, the tangent program) lies inside the store the
   kernel gives that program, checked here from the emitted tables instead
   of by bounds checks on the device.
 """
@@ -110,10 +110,12 @@ def test_program_slots_lie_inside_their_stores(path):
     coop, adj, tlm = (_int_const(text, n) for n in ("COOP_SLOTS", "NSLOTS_ADJ", "NSLOTS_TLM"))
     sched = _words(text, "sched")
     assert sched and _max_slot(sched) < coop
-    adj_prog = _words(text, "adj_prog")
-    assert (adj_prog is not None) == ("TABLE_ATTEMPT = true" in text)
-    if adj_prog is not None:                      # table-driven adjoint
+    table = "TABLE_ATTEMPT = true" in text
+    adj_prog, eval_prog = _words(text, "adj_prog"), _words(text, "eval_prog")
+    assert (adj_prog is not None) == table and (eval_prog is not None) == table
+    if table:                                     # table-driven adjoint and evaluation
         assert _max_slot(adj_prog) < adj
+        assert _max_slot(eval_prog) < coop and coop == _int_const(text, "NSLOTS")
     tlm_prog = _words(text, "tlm_prog")
     assert tlm_prog and _max_slot(tlm_prog) < tlm
     assert _int_const(text, "TLM_CB") + _int_const(text, "TLM_NCONST") <= tlm

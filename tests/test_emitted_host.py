@@ -21,6 +21,8 @@ same Troe rates), which get the first two checks too.
 import ctypes as C
 from fractions import Fraction
 
+from pathlib import Path
+
 import hostsim_lib
 import numpy as np
 import pytest
@@ -480,3 +482,43 @@ def test_emitted_tendencies_and_jacobian_match_reference(hostsim, mech):
         nz = J0[:, :, c] != 0
         assert not np.any(J[~nz])
         assert (np.abs(J - J0[:, :, c])[nz] / np.abs(J0[:, :, c][nz])).max() < 1e-11
+
+
+def test_ts1_table_evaluation_matches_reference_fixture(hostsim):
+    """TS1's table-driven evaluation program (eval_step: the partials, W with
+    1/(gamma h) = 0 and F, walked by one thread) with the emitted rate
+    constants and fixed-species columns, against the reference's own
+    generated TS1 compute_rates / compute_jacobian
+    (tests/golden/ts1_reference_rates.json, at the inputs of its native TS1
+    run, photolysis scaled by 1.0 and 1.05): F to 1e-13 of the largest |F|,
+    every nonzero J entry to 1e-11, zeros where the reference writes none."""
+    import json
+
+    lib = hostsim["ts1"]
+    lib.hostsim_rate_constants.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_void_p]
+    lib.hostsim_evaluate.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_void_p, C.c_void_p, C.c_void_p]
+    here = Path(__file__).resolve().parent / "golden"
+    g = json.loads((here / "ts1_kokkos_2x300.json").read_text())
+    rates = json.loads((here / "ts1_reference_rates.json").read_text())
+    conc = np.ascontiguousarray(g["initial"], dtype=np.float64)
+    ns, nr = len(conc), len(load("ts1").reactions)
+    for case in rates["cases"]:
+        prm = np.array(g["parameters"], dtype=np.float64)
+        prm[:g["photolysis_slots"]] *= case["photolysis_scale"]
+        k = np.zeros(nr)
+        lib.hostsim_rate_constants(conc.ctypes.data, prm.ctypes.data, g["temperature"], g["air_density"],
+                                   g["rh"], 0.0, k.ctypes.data)
+        F, J = np.zeros(ns), np.zeros(ns * ns)
+        assert lib.hostsim_evaluate(conc.ctypes.data, prm.ctypes.data, g["temperature"], g["air_density"],
+                                    g["rh"], 0.0, k.ctypes.data, F.ctypes.data, J.ctypes.data) == 0
+        J = J.reshape(ns, ns).T                       # [row, col]
+        F0 = np.array(case["F"])
+        assert np.abs(F - F0).max() <= 1e-13 * np.abs(F0).max()
+        J0 = np.zeros((ns, ns))
+        for i, j, v in case["J"]:
+            J0[i, j] = v
+        nz = J0 != 0
+        assert not np.any(J[~nz])
+        assert (np.abs(J - J0)[nz] / np.abs(J0[nz])).max() < 1e-11

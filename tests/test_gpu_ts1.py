@@ -13,8 +13,8 @@ Here:
   to 1e3 so that the comparison measures the arithmetic rather than the
   conditioning.  Even then ~20% of the synthetic cells end non-finite on
   both sides;
-* the evaluation entries, not built for table-driven libraries, answer
-  MKPP_ERROR_INVALID_STATE.
+* the evaluation entries, table-driven too (one sequential program per
+  cell for the partials, W and F), against the oracle.
 """
 import numpy as np
 import pytest
@@ -76,17 +76,26 @@ def test_ts1_forced_step_sequence_parity(ts1_lib):
     assert (np.abs(got - ref) / (np.abs(ref) + atol)).max() <= 1e-9
 
 
-def test_ts1_evaluation_entries_report_unavailable(ts1_lib):
-    from mkpp_gb300.api import MechanismContext, MkppError
+def test_ts1_tendencies_and_jacobian(ts1_lib):
+    """The table-driven evaluation entries (mkpp_evaluate_rates /
+    mkpp_evaluate_jacobian: Mech::eval_step per cell, then the fixed-species
+    columns) against the oracle: 1e-10 of the cell's largest entry, as for
+    the unrolled mechanisms."""
+    from mkpp_gb300.api import MechanismContext
 
     w = workloads.make("ts1", 4)
+    o = Oracle("ts1")
+    F_ref, J_ref = o.evaluate(w.conc, w.temp, w.rho, w.rh, None, w.param)
+    Jd_ref = o.dense_jacobian(J_ref)          # [row, col, cell]
     ctx = MechanismContext("ts1", 4)
     try:
         ctx.set_state(np.ascontiguousarray(w.conc), w.temp.copy(), w.pressure.copy(), w.rho.copy())
         ctx.set_aerosol(relative_humidity=w.rh.copy())
         ctx.set_rate_parameters(np.ascontiguousarray(w.param))
-        with pytest.raises(MkppError) as e:
-            ctx.evaluate_rates()
-        assert e.value.code == -104 and "table-driven" in str(e.value)
+        F = ctx.evaluate_rates()
+        J = ctx.evaluate_jacobian()            # [col, row, cell]
     finally:
         ctx.close()
+    assert np.all(np.abs(F - F_ref) <= 1e-10 * (np.abs(F_ref).max(axis=0) + 1e-300))
+    Jt = np.transpose(J, (1, 0, 2))
+    assert np.all(np.abs(Jt - Jd_ref) <= 1e-10 * (np.abs(Jd_ref).max(axis=(0, 1)) + 1e-300))
