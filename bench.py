@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
     ap.add_argument("--adjoint-cells", type=int, default=65536, help="cells of the adjoint/forward measurement")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--tangent", type=int, default=0,
+                    help="also time the tangent sweep over the adjoint section's checkpoints (mkpp_gpu_tangent)")
     ap.add_argument("--tail-after", type=int, default=0,
                     help="tail parking threshold in attempts for every integrate launch (mkpp_set_tail_parking; 0 off)")
     ap.add_argument("--e2e-cost-order", type=int, default=0,
@@ -485,7 +487,26 @@ def main():
                 "finite_gradients_frac": float(torch.isfinite(gc).all(0).double().mean()),
             }
             log(f"adjoint: forward {fms:.0f} ms, adjoint {ams:.0f} ms, ratio {ams / fms:.2f}")
-            del ck, gc, gk
+            del gc, gk
+            if args.tangent:
+                # Forward sensitivities over the same checkpoints: a direction in
+                # every initial concentration and every rate constant, scaled by
+                # their values (mkpp_gpu_tangent).
+                gen = torch.Generator(device="cpu").manual_seed(2719)
+                dc = (ca0 * (2 * torch.rand(ca0.shape, generator=gen, dtype=f64).to(dev) - 1)).contiguous()
+                dk = (ka * (2 * torch.rand(ka.shape, generator=gen, dtype=f64).to(dev) - 1)).contiguous()
+                ev_t = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                with torch.cuda.stream(stream):
+                    ev_t[0].record(stream)
+                    tan = ck.tangent(ka, dc, dk)
+                    ev_t[1].record(stream)
+                    stream.synchronize()
+                tms = ev_t[0].elapsed_time(ev_t[1])
+                result["adjoint"].update({"tangent_ms": tms, "tangent_over_forward": tms / fms,
+                                          "finite_tangent_frac": float(torch.isfinite(tan).all(0).double().mean())})
+                log(f"tangent: {tms:.0f} ms, ratio {tms / fms:.2f}")
+                del tan, dc, dk
+            del ck
             torch.cuda.empty_cache()
 
     if not args.no_e2e:
