@@ -106,6 +106,12 @@ int mkpp_mechanism_name(const char** name_out);
 /* species, variable species, reactions, runtime parameter slots, LU slots */
 int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions,
                          int* num_rate_parameters, int* num_lu_slots);
+/* SUPPORTS_RUNTIME_ENVIRONMENT and HAS_CLOUD_GATED of the reference's
+ * SolverKernels (header.j2:127-186) as 0/1; either pointer may be NULL. */
+int mkpp_mechanism_flags(int* runtime_environment, int* cloud_gated);
+/* SolverKernels::atol[] / rtol[]: NS values each, physical species order;
+ * either pointer may be NULL. */
+int mkpp_mechanism_tolerances(double* atol, double* rtol);
 
 /* ---- Device-pointer entry points (no reference counterpart) ----------- */
 

@@ -86,6 +86,8 @@ SIGNATURES = [
     ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_set_cost_order", _i, [_vp, _i]),
+    ("mkpp_mechanism_flags", _i, [_vp, _vp]),
+    ("mkpp_mechanism_tolerances", _i, [_vp, _vp]),
     ("mkpp_set_tail_parking", _i, [_i]),
     ("mkpp_gpu_tangent_workspace_bytes", _sz, [_sz]),
     ("mkpp_gpu_tangent", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

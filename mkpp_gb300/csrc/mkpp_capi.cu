@@ -687,6 +687,22 @@ int mkpp_mechanism_sizes(int* num_species, int* num_variable, int* num_reactions
   return MKPP_SUCCESS;
 }
 
+int mkpp_mechanism_flags(int* runtime_environment, int* cloud_gated) {
+  if (!runtime_environment && !cloud_gated) return MKPP_ERROR_NULL_POINTER;
+  if (runtime_environment) *runtime_environment = Mech::RUNTIME_ENV ? 1 : 0;
+  if (cloud_gated) *cloud_gated = Mech::CLOUD_GATED ? 1 : 0;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_mechanism_tolerances(double* atol, double* rtol) {
+  if (!atol && !rtol) return MKPP_ERROR_NULL_POINTER;
+  for (int s = 0; s < Mech::NS; ++s) {
+    if (atol) atol[s] = Mech::ATOL[s];
+    if (rtol) rtol[s] = Mech::RTOL[s];
+  }
+  return MKPP_SUCCESS;
+}
+
 // ---- Device-pointer entry points --------------------------------------------
 
 size_t mkpp_gpu_workspace_bytes(size_t num_cells) { return workspace_bytes(num_cells); }

@@ -1158,6 +1158,10 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
       + ", ".join(_lit(plan.atol[p]) for p in plan.var_phys) + "}; return t[i]; }")
     c(f"  __host__ __device__ static constexpr double rtol_v(int i) {{ constexpr double t[{nv}] = {{"
       + ", ".join(_lit(plan.rtol[p]) for p in plan.var_phys) + "}; return t[i]; }")
+    # Tolerances of every species in physical order, the reference's
+    # SolverKernels::atol[] / rtol[] (host queries; the solve uses the above).
+    c(f"  static constexpr double ATOL[NS] = {{" + ", ".join(_lit(x) for x in plan.atol) + "};")
+    c(f"  static constexpr double RTOL[NS] = {{" + ", ".join(_lit(x) for x in plan.rtol) + "};")
     c(f"  __host__ __device__ static constexpr int lu_prow(int s) {{ constexpr int t[{nlu}] = {{"
       + ", ".join(str(plan.var_phys[r]) for r, _ in plan.lu_slots) + "}; return t[s]; }")
     c(f"  __host__ __device__ static constexpr int lu_pcol(int s) {{ constexpr int t[{nlu}] = {{"

@@ -255,6 +255,8 @@ struct Mech {
   __host__ __device__ static constexpr int fix_phys(int i) { constexpr int t[1] = {3}; return t[i]; }
   __host__ __device__ static constexpr double atol_v(int i) { constexpr double t[3] = {1.0, 1.0, 1.0}; return t[i]; }
   __host__ __device__ static constexpr double rtol_v(int i) { constexpr double t[3] = {0.001, 0.001, 0.001}; return t[i]; }
+  static constexpr double ATOL[NS] = {1.0, 1.0, 1.0, 1.0};
+  static constexpr double RTOL[NS] = {0.001, 0.001, 0.001, 0.001};
   __host__ __device__ static constexpr int lu_prow(int s) { constexpr int t[9] = {2, 2, 2, 0, 0, 0, 1, 1, 1}; return t[s]; }
   __host__ __device__ static constexpr int lu_pcol(int s) { constexpr int t[9] = {2, 0, 1, 2, 0, 1, 2, 0, 1}; return t[s]; }
   static const char* species_name(int s) { static const char* t[4] = {"O", "O2", "O3", "M"}; return t[s]; }

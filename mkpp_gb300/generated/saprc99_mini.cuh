@@ -628,6 +628,8 @@ struct Mech {
   __host__ __device__ static constexpr int fix_phys(int i) { constexpr int t[3] = {12, 15, 16}; return t[i]; }
   __host__ __device__ static constexpr double atol_v(int i) { constexpr double t[14] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0}; return t[i]; }
   __host__ __device__ static constexpr double rtol_v(int i) { constexpr double t[14] = {0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001}; return t[i]; }
+  static constexpr double ATOL[NS] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
+  static constexpr double RTOL[NS] = {0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001};
   __host__ __device__ static constexpr int lu_prow(int s) { constexpr int t[53] = {14, 8, 6, 13, 13, 13, 13, 11, 1, 1, 10, 10, 10, 10, 0, 0, 0, 0, 0, 0, 7, 7, 2, 2, 2, 2, 2, 2, 9, 9, 9, 9, 9, 9, 9, 4, 4, 4, 4, 4, 4, 4, 4, 3, 3, 3, 3, 3, 3, 3, 5, 5, 5}; return t[s]; }
   __host__ __device__ static constexpr int lu_pcol(int s) { constexpr int t[53] = {14, 8, 6, 13, 11, 0, 9, 11, 11, 1, 6, 1, 10, 7, 13, 11, 0, 2, 9, 3, 10, 7, 6, 0, 2, 9, 4, 3, 13, 11, 0, 2, 9, 4, 3, 10, 0, 7, 2, 9, 4, 3, 5, 0, 7, 2, 9, 4, 3, 5, 4, 3, 5}; return t[s]; }
   static const char* species_name(int s) { static const char* t[17] = {"O3", "H2O2", "NO", "NO2", "NO3", "N2O5", "HONO", "HNO3", "HNO4", "O3P", "OH", "HO2", "AIR", "O2", "H2O", "M", "N2"}; return t[s]; }

@@ -475,6 +475,8 @@ struct Mech {
   __host__ __device__ static constexpr int fix_phys(int i) { constexpr int t[1] = {5}; return t[i]; }
   __host__ __device__ static constexpr double atol_v(int i) { constexpr double t[6] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0}; return t[i]; }
   __host__ __device__ static constexpr double rtol_v(int i) { constexpr double t[6] = {0.001, 0.001, 0.001, 0.001, 0.001, 0.001}; return t[i]; }
+  static constexpr double ATOL[NS] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
+  static constexpr double RTOL[NS] = {0.001, 0.001, 0.001, 0.001, 0.001, 0.001, 0.001};
   __host__ __device__ static constexpr int lu_prow(int s) { constexpr int t[29] = {1, 1, 0, 0, 0, 0, 0, 6, 6, 6, 6, 6, 6, 2, 2, 2, 2, 2, 2, 3, 3, 3, 3, 3, 4, 4, 4, 4, 4}; return t[s]; }
   __host__ __device__ static constexpr int lu_pcol(int s) { constexpr int t[29] = {1, 2, 1, 0, 6, 2, 4, 1, 0, 6, 2, 3, 4, 1, 0, 6, 2, 3, 4, 0, 6, 2, 3, 4, 0, 6, 2, 3, 4}; return t[s]; }
   static const char* species_name(int s) { static const char* t[7] = {"O", "O1D", "O3", "NO", "NO2", "M", "O2"}; return t[s]; }

@@ -194,3 +194,27 @@ def test_reference_cpp_wrapper_and_sizes(mech, tmp_path):
                     f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0 and out.stdout.strip() == "ok", (out.returncode, out.stderr)
+
+
+@pytest.mark.parametrize("mech", ["chapman", "ts1"])
+def test_mechanism_flags_and_tolerances(mech):
+    """mkpp_mechanism_flags / mkpp_mechanism_tolerances give the reference's
+    SolverKernels constants (SUPPORTS_RUNTIME_ENVIRONMENT, HAS_CLOUD_GATED,
+    atol[] and rtol[] in physical species order) from the plan."""
+    from mkpp_gb300 import api, build
+    from mkpp_gb300.emitter.plan import load_raw
+
+    try:
+        build.build((mech,))
+    except RuntimeError as e:  # no nvcc
+        pytest.skip(str(e))
+    lib = api.load_library(mech)
+    raw = load_raw(mech)
+    env, cloud = C.c_int(-1), C.c_int(-1)
+    assert lib.mkpp_mechanism_flags(C.byref(env), C.byref(cloud)) == 0
+    assert (env.value, cloud.value) == (int(raw["runtime_environment"]), int(raw["cloud_gated"]))
+    assert lib.mkpp_mechanism_flags(None, None) == -101
+    ns = len(raw["species"])
+    atol, rtol = np.zeros(ns), np.zeros(ns)
+    assert lib.mkpp_mechanism_tolerances(atol.ctypes.data, rtol.ctypes.data) == 0
+    assert atol.tolist() == raw["atol"] and rtol.tolist() == raw["rtol"]
