@@ -1,5 +1,7 @@
 // Pieces of the tendency and dense-Jacobian evaluation shared by the unrolled
 // (mkpp_eval.cu) and the table-driven (mkpp_eval_table.cu) evaluation units.
+// A library links exactly one of the two, so the kernel defined here exists
+// once per library.
 #pragma once
 #include "capi_common.cuh"
 
