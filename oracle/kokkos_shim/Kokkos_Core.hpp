@@ -1,5 +1,5 @@
 // Minimal host-only stand-in for the Kokkos API surface that MKPP's generated
-// solver headers use (TEST AND BASELINE INFRASTRUCTURE ONLY; no Kokkos exists
+// solver headers use (TEST AND CPU-BASELINE INFRASTRUCTURE ONLY; no Kokkos exists
 // on this image).  It provides:
 //   * View<DataType, Props...> for rank 1 and 2 over caller memory, with
 //     LayoutLeft / LayoutRight / LayoutStride strides, data(), stride(),

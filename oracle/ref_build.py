@@ -1,4 +1,4 @@
-"""Build the reference's own CPU solver (TEST AND BASELINE INFRASTRUCTURE ONLY).
+"""Build the reference's own CPU solver (TEST AND CPU-BASELINE INFRASTRUCTURE ONLY).
 
 Recipe, run where the MKPP reference checkout exists (it is never copied
 into the repository):

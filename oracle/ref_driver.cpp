@@ -1,4 +1,4 @@
-// Driver of the reference's generated CPU solver (TEST AND BASELINE
+// Driver of the reference's generated CPU solver (TEST AND CPU-BASELINE
 // INFRASTRUCTURE ONLY).  Compiled by oracle/ref_build.py against the headers
 // the MKPP compiler regenerated into oracle/_ref/gen/<mech>/ and the Kokkos
 // shim.  For every cell it binds the state as a strided view of the
