@@ -81,6 +81,13 @@ int mkpp_integrate(mkpp_handle_t handle, double dt);
 int mkpp_evaluate_rates(mkpp_handle_t handle, double* rates_out);
 /* mkpp.h.j2:71: dense Jacobian (cells x N x N) LayoutLeft. */
 int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out);
+/* Products with that Jacobian, the per-cell quantities of the reference's
+ * SolverKernels::compute_tlm (dF = J delta,
+ * src/mkpp/templates/kernel_functions/compute_tlm.j2) and compute_adjoint
+ * (J^T, compute_adjoint.j2) applied to a vector: out = J delta or J^T lambda,
+ * all (cells x species) LayoutLeft host arrays (no reference C entry). */
+int mkpp_evaluate_jacobian_vector(mkpp_handle_t handle, const double* delta, double* out);
+int mkpp_evaluate_jacobian_transpose_vector(mkpp_handle_t handle, const double* lambda, double* out);
 /* mkpp.h.j2:74 */
 int mkpp_get_last_error(mkpp_handle_t handle, char* buffer, size_t buffer_len);
 

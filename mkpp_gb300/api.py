@@ -66,6 +66,8 @@ SIGNATURES = [
     ("mkpp_integrate", _i, [_vp, _d]),
     ("mkpp_evaluate_rates", _i, [_vp, _vp]),
     ("mkpp_evaluate_jacobian", _i, [_vp, _vp]),
+    ("mkpp_evaluate_jacobian_vector", _i, [_vp, _vp, _vp]),
+    ("mkpp_evaluate_jacobian_transpose_vector", _i, [_vp, _vp, _vp]),
     ("mkpp_get_last_error", _i, [_vp, C.c_char_p, _sz]),
     ("mkpp_set_initial_step_seed", _i, [_vp, _d]),
     ("mkpp_set_max_attempts", _i, [_vp, _i]),
@@ -249,6 +251,14 @@ class MechanismContext:
         ns = self.sizes.species
         out = np.zeros((ns, ns, self.num_cells))
         self._check(self.lib.mkpp_evaluate_jacobian(self.handle, _ptr(out)))
+        return out
+
+    def evaluate_jacobian_vector(self, delta, transpose: bool = False) -> np.ndarray:
+        """J delta (or J^T delta) per cell, (species, cells) arrays."""
+        delta = self._host(delta, (self.sizes.species, self.num_cells))
+        out = np.zeros((self.sizes.species, self.num_cells))
+        fn = self.lib.mkpp_evaluate_jacobian_transpose_vector if transpose else self.lib.mkpp_evaluate_jacobian_vector
+        self._check(fn(self.handle, _ptr(delta), _ptr(out)))
         return out
 
     def cell_stats(self):

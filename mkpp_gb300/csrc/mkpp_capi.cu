@@ -628,6 +628,69 @@ int mkpp_evaluate_jacobian(mkpp_handle_t handle, double* jac_out) {
   return MKPP_SUCCESS;
 }
 
+// out = J v or J^T v per cell on the dense (cells x N x N) LayoutLeft Jacobian
+// jac[c + n (row + N col)]; v and out are (cells x N) LayoutLeft.
+static __global__ void jac_vec_kernel(size_t n, const double* jac, const double* v, double* out, bool transpose) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const size_t NS = Mech::NS;
+  for (size_t i = 0; i < NS; ++i) {
+    double acc = 0.0;
+    for (size_t j = 0; j < NS; ++j) {
+      const double jij = transpose ? jac[c + n * (j + NS * i)] : jac[c + n * (i + NS * j)];
+      acc = fma(jij, v[c + n * j], acc);
+    }
+    out[c + n * i] = acc;
+  }
+}
+
+// The dense Jacobian of the bound state (as mkpp_evaluate_jacobian) applied
+// to a host vector, or its transpose.
+static int jacobian_product(mkpp_handle_t handle, const double* vec, double* out, bool transpose) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  mkpp_handle_s* h = handle;
+  if (!vec || !out) {
+    h->set_error("FATAL ERROR: Jacobian product vector or output pointer is null");
+    return MKPP_ERROR_NULL_POINTER;
+  }
+  if (!h->initialized) {
+    h->set_error("FATAL ERROR: MKPP handle must be initialized before Jacobian evaluation");
+    return MKPP_ERROR_INVALID_STATE;
+  }
+  const int vs = validate_state(*h);
+  if (vs != MKPP_SUCCESS) return vs;
+  const size_t n = h->num_cells;
+  const size_t jbytes = n * Mech::NS * Mech::NS * sizeof(double);
+  const size_t vbytes = n * Mech::NS * sizeof(double);
+  int rc = ensure_device(h, jbytes + 2 * vbytes);
+  if (rc != MKPP_SUCCESS) return rc;
+  rc = stage_inputs(h);
+  if (rc != MKPP_SUCCESS) return rc;
+  DeviceBuffers& d = h->dev;
+  if (launch_eval_jacobian(n, d.conc, d.ktab, d.out, h->stream) != MKPP_SUCCESS)
+    return device_fail(h, cudaGetLastError(), "eval_jacobian_kernel launch");
+  if (Mech::NFIX > 0 &&
+      launch_fixed_columns(n, d.conc, d.temp, d.rho, h->rh ? d.rh : nullptr, h->clw ? d.clw : nullptr,
+                           h->param ? d.param : nullptr, d.out, h->stream) != MKPP_SUCCESS)
+    return device_fail(h, cudaGetLastError(), "fixed_columns_kernel launch");
+  double* dv = d.out + n * Mech::NS * Mech::NS;
+  double* dres = dv + n * Mech::NS;
+  MKPP_CUDA(h, cudaMemcpyAsync(dv, vec, vbytes, cudaMemcpyHostToDevice, h->stream));
+  jac_vec_kernel<<<launch_grid(n, 128), 128, 0, h->stream>>>(n, d.out, dv, dres, transpose);
+  MKPP_CUDA(h, cudaGetLastError());
+  MKPP_CUDA(h, cudaMemcpyAsync(out, dres, vbytes, cudaMemcpyDeviceToHost, h->stream));
+  MKPP_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MKPP_SUCCESS;
+}
+
+int mkpp_evaluate_jacobian_vector(mkpp_handle_t handle, const double* delta, double* out) {
+  return jacobian_product(handle, delta, out, false);
+}
+
+int mkpp_evaluate_jacobian_transpose_vector(mkpp_handle_t handle, const double* lambda, double* out) {
+  return jacobian_product(handle, lambda, out, true);
+}
+
 int mkpp_get_last_error(mkpp_handle_t handle, char* buffer, size_t buffer_len) {
   if (!handle || !buffer || buffer_len == 0) return MKPP_ERROR_NULL_POINTER;
   std::strncpy(buffer, handle->last_error.c_str(), buffer_len - 1);

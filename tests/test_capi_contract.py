@@ -113,6 +113,10 @@ def test_state_binding_and_argument_errors(lib):
         t[2] = 298.15
         assert lib.mkpp_evaluate_rates(h, None) == -101
         assert lib.mkpp_evaluate_jacobian(h, None) == -101
+        v = np.zeros((4, n))
+        assert lib.mkpp_evaluate_jacobian_vector(h, None, ptr(v)) == -101
+        assert lib.mkpp_evaluate_jacobian_transpose_vector(h, ptr(v), None) == -101
+        assert lib.mkpp_evaluate_jacobian_vector(None, ptr(v), ptr(v)) == -101
     finally:
         assert lib.mkpp_destroy_handle(h) == 0
 

@@ -140,3 +140,32 @@ def test_heterogeneous_batch_equals_single_cells(lib, built_libs, mech):
         assert e.value.code == -103
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("mech", ["chapman", MECH])
+def test_jacobian_vector_products(lib, built_libs, mech):
+    """mkpp_evaluate_jacobian_vector / _transpose_vector (the per-cell J delta
+    of the reference's compute_tlm and J^T lambda of compute_adjoint) equal
+    the dense Jacobian of mkpp_evaluate_jacobian applied on the host, to
+    1e-13 of the sum of the absolute terms (the summation orders differ)."""
+    from mkpp_gb300.api import MechanismContext
+
+    n = 16
+    w = workloads.make(mech, n)
+    rng = np.random.default_rng(4)
+    v = np.ascontiguousarray(rng.uniform(-1.0, 1.0, w.conc.shape))
+    ctx = MechanismContext(mech, n)
+    try:
+        ctx.set_state(np.ascontiguousarray(w.conc), w.temp.copy(), w.pressure.copy(), w.rho.copy())
+        ctx.set_aerosol(relative_humidity=w.rh.copy())
+        ctx.set_rate_parameters(np.ascontiguousarray(w.param))
+        J = np.transpose(ctx.evaluate_jacobian(), (2, 1, 0))     # [cell, row, col]
+        jv = ctx.evaluate_jacobian_vector(v)
+        jtv = ctx.evaluate_jacobian_vector(v, transpose=True)
+    finally:
+        ctx.close()
+    vc = v.T                                                      # [cell, species]
+    ref = np.einsum("cij,cj->ic", J, vc)
+    ref_t = np.einsum("cji,cj->ic", J, vc)
+    assert np.all(np.abs(jv - ref) <= 1e-13 * np.einsum("cij,cj->ic", np.abs(J), np.abs(vc)) + 1e-300)
+    assert np.all(np.abs(jtv - ref_t) <= 1e-13 * np.einsum("cji,cj->ic", np.abs(J), np.abs(vc)) + 1e-300)
