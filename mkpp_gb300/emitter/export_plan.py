@@ -303,10 +303,14 @@ def main(argv=None) -> int:
     ap.add_argument("--solver", default="ros3")
     ap.add_argument("--temperature", type=float, default=298.15)
     ap.add_argument("--air-density", type=float, default=2.46e19)
+    ap.add_argument("--name", default=None,
+                    help="library name, for a second build of a mechanism (e.g. at other tolerances)")
     args = ap.parse_args(argv)
     os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
     plan = export(args.mkpp_src, args.mechanism, args.rtol, args.atol, args.solver, args.seed,
                   args.temperature, args.air_density)
+    if args.name:
+        plan["name"] = args.name
     Path(args.out).parent.mkdir(parents=True, exist_ok=True)
     with open(args.out, "w") as f:
         json.dump(plan, f, separators=(",", ":"))

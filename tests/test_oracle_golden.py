@@ -94,3 +94,16 @@ def test_oracle_flags_non_finite_cell():
     out = Oracle("chapman").integrate(conc, w.dt, param=w.param)
     assert out["status"][5] == 2
     assert np.all(np.delete(out["status"], 5) == 0)
+
+
+def test_chapman_shipped_plan_reproduces_native_run():
+    """The chapman_shipped plan (Chapman exported at the shipped tolerances,
+    the plan of the GPU library that tests/test_gpu_golden.py runs) gives the
+    reference's native-run final state through the oracle, to 1e-14."""
+    g = json.loads((GOLD / "chapman_kokkos_10x60.json").read_text())
+    o = Oracle("chapman_shipped")
+    names = o.raw["species"]
+    conc = np.array([[g["initial"][s]] for s in names])
+    out = o.integrate(conc, g["dt"], steps=g["steps"], param=np.array(g["jvals"])[:, None])
+    want = np.array([g["final"][s] for s in names])
+    np.testing.assert_allclose(out["conc"][:, 0], want, rtol=1e-14, atol=0)

@@ -77,3 +77,17 @@ def test_tableaux_match_reference_coefficients():
     assert tab["C"] == [-1.0156171083877703, 4.07599564525377, 9.20767942983308]
     assert tab["M"] == [1.0, 6.1697947043828245, -0.42772256543218573]
     assert tab["NewF"] == [True, True, False]
+
+
+def test_tolerance_variant_differs_only_in_name_and_tolerances():
+    """chapman_shipped is the Chapman plan exported at the shipped header's
+    tolerances (mkpp-generated/chapman.hpp: rtol 1e-6, atol 1e-3), the
+    settings of the reference's native-run golden output; its emitted
+    headers are current."""
+    a, b = load_raw("chapman"), load_raw("chapman_shipped")
+    assert sorted(k for k in a if a[k] != b[k]) == ["atol", "name", "rtol"]
+    assert set(b["rtol"]) == {1e-6} and set(b["atol"]) == {1e-3}
+    plan = load("chapman_shipped")
+    assert (cuda_emitter.GEN_DIR / "chapman_shipped.cuh").read_text() == cuda_emitter.emit_mechanism(plan)
+    assert ((cuda_emitter.GEN_DIR / "host_api" / "chapman_shipped" / "mkpp.h").read_text()
+            == cuda_emitter.emit_host_header(plan))
