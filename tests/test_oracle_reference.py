@@ -174,3 +174,21 @@ def test_ts1_oracle_runs_the_native_schedule():
         conc = r["conc"]
         assert np.all(r["status"] == 0)
     assert np.isfinite(conc).all()
+
+
+@pytest.mark.parametrize("mech", ["small_strato", "saprc99"])
+def test_reference_and_oracle_are_thread_count_independent(mech):
+    """The reference's determinism test (tests/integration/e2e_validation/
+    test_determinism.cpp:166-180: bit-identical results with 1 and 8 OpenMP
+    threads) does not build here (its submodule is absent).  The same
+    property of the reference's own generated solver built here, and of the
+    oracle: one host step of 64 seeded cells with 1 and with 8 threads, bit
+    for bit."""
+    ref = _ref(mech)
+    o = Oracle(mech)
+    w = workloads.make(mech, 64)
+    P = w.param_at(0)
+    for solver in (ref, o):
+        runs = [solver.integrate(w.conc.copy(), w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P,
+                                 nthreads=t)["conc"] for t in (1, 8)]
+        assert np.array_equal(runs[0], runs[1], equal_nan=True)
