@@ -103,6 +103,12 @@ def test_state_binding_and_argument_errors(lib):
         assert lib.mkpp_set_cloud_water_ptr(h, ptr(np.zeros(n))) == 0
         status = np.zeros(n, np.int32)
         assert lib.mkpp_get_cell_stats(h, ptr(status), None, None) == -104
+        assert lib.mkpp_set_initial_step_seed(None, C.c_double(1e-6)) == -101
+        for bad in (0.0, -1e-6, float("nan"), float("inf")):
+            assert lib.mkpp_set_initial_step_seed(h, C.c_double(bad)) == -103
+        assert "initial_step_seed" in _error(lib, h)
+        assert lib.mkpp_set_initial_step_seed(h, C.c_double(1e-5)) == 0
+        assert lib.mkpp_set_max_attempts(h, 0) == -103 and lib.mkpp_set_max_attempts(h, 5000) == 0
         assert lib.mkpp_set_cost_order(None, 1) == -101
         assert lib.mkpp_set_cost_order(h, 1) == 0 and lib.mkpp_set_cost_order(h, 0) == 0
         assert lib.mkpp_integrate(h, C.c_double(0.0)) == -103

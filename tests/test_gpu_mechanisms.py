@@ -169,3 +169,34 @@ def test_jacobian_vector_products(lib, built_libs, mech):
     ref_t = np.einsum("cji,cj->ic", J, vc)
     assert np.all(np.abs(jv - ref) <= 1e-13 * np.einsum("cij,cj->ic", np.abs(J), np.abs(vc)) + 1e-300)
     assert np.all(np.abs(jtv - ref_t) <= 1e-13 * np.einsum("cji,cj->ic", np.abs(J), np.abs(vc)) + 1e-300)
+
+
+def test_initial_step_seed_is_honoured(built_libs):
+    """mkpp_set_initial_step_seed (the reference's SolverKernels::
+    initial_step_seed member, integrate.j2:42; its test_initial_step_seed.py
+    checks the plumbing): a larger seed changes the attempt counts, and the
+    result agrees with the oracle run at the same seed within the
+    free-running bound (10 (rtol |o| + atol))."""
+    from mkpp_gb300.api import MechanismContext
+
+    n = 64
+    w = workloads.make("chapman", n)
+    o = Oracle("chapman")
+    out = {}
+    for seed in (None, 1e-3):
+        host = np.ascontiguousarray(w.conc.copy())
+        ctx = MechanismContext("chapman", n)
+        try:
+            if seed is not None:
+                ctx.set_initial_step_seed(seed)
+            ctx.set_state(host, w.temp.copy(), w.pressure.copy(), w.rho.copy())
+            ctx.set_rate_parameters(np.ascontiguousarray(w.param))
+            ctx.integrate(w.dt)
+            st, acc, rej = ctx.cell_stats()
+        finally:
+            ctx.close()
+        out[seed] = (host, acc + rej)
+    assert not np.array_equal(out[None][1], out[1e-3][1])
+    ref = o.integrate(w.conc.copy(), w.dt, param=w.param, seed=1e-3)
+    tol = np.array(o.raw["rtol"])[:, None] * np.abs(ref["conc"]) + np.array(o.raw["atol"])[:, None]
+    assert np.all(np.abs(out[1e-3][0] - ref["conc"]) <= 10 * tol)
