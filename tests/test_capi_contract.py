@@ -228,3 +228,29 @@ def test_mechanism_flags_and_tolerances(mech):
     atol, rtol = np.zeros(ns), np.zeros(ns)
     assert lib.mkpp_mechanism_tolerances(atol.ctypes.data, rtol.ctypes.data) == 0
     assert atol.tolist() == raw["atol"] and rtol.tolist() == raw["rtol"]
+
+
+def test_device_entry_argument_checks(lib):
+    """The device-pointer entries reject bad arguments before touching the
+    device: null pointers -101; zero cells, more than INT32_MAX cells, and
+    non-positive dt, steps, seed or attempt cap -103; a parameter count other
+    than the mechanism's -103.  No pointer here is dereferenced."""
+    buf = np.zeros(64)
+    p = buf.ctypes.data
+    big = 2 ** 31
+    integ = lambda n, conc=p, steps=1, dt=60.0, seed=1e-6, cap=100: lib.mkpp_gpu_integrate_k(  # noqa: E731
+        n, conc, p, 0, steps, dt, seed, cap, 1, None, None, None, None, p, 1 << 30, None)
+    assert integ(4, conc=None) == -101
+    assert integ(0) == -103 and integ(big) == -103
+    assert integ(4, steps=0) == -103 and integ(4, dt=0.0) == -103 and integ(4, dt=float("nan")) == -103
+    assert integ(4, seed=0.0) == -103 and integ(4, cap=0) == -103
+    assert lib.mkpp_gpu_rate_constants(4, None, p, p, None, None, p, 2, p, None, None) == -101
+    assert lib.mkpp_gpu_rate_constants(0, p, p, p, None, None, p, 2, p, None, None) == -103
+    assert lib.mkpp_gpu_rate_constants(4, p, p, p, None, None, p, 3, p, None, None) == -103
+    assert lib.mkpp_gpu_tangent(4, p, 8, None, p, p, p, None, p, p, 1 << 30, None) == -101
+    assert lib.mkpp_gpu_tangent(0, p, 8, p, p, p, p, None, p, p, 1 << 30, None) == -103
+    assert lib.mkpp_gpu_adjoint(4, p, 0, p, p, p, p, p, p, p, 1 << 30, None) == -103
+    assert lib.mkpp_gpu_evaluate_rates(0, p, p, p, None) == -103
+    assert lib.mkpp_gpu_evaluate_jacobian(4, None, p, p, None) == -101
+    h = C.c_void_p()
+    assert lib.mkpp_create_handle(C.byref(h), big) == -103
