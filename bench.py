@@ -536,6 +536,11 @@ def main():
             log(f"e2e: {e2e_s:.1f} s")
             h2d = hs * n * 8 * (NS + 3 + NP)
             d2h = hs * n * 8 * NS
+            if args.e2e_cost_order:
+                # Every call after the first sends the cell order (int32) and
+                # every call reads back the accepted and rejected counts.
+                h2d += (hs - 1) * n * 4
+                d2h += hs * n * 8
             result["e2e"] = {"value": cell_solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                              "d2h_bytes_per_step": d2h, "path": "mkpp_set_rate_parameter_ptrs + mkpp_integrate x 24",
                              "cost_order": bool(args.e2e_cost_order)}
