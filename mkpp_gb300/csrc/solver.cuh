@@ -507,6 +507,10 @@ struct CheckpointArgs {
   double* y;
   double* h;
   int* n;
+  // Recorded steps of cell c as the sweeps read them: the forward writes at
+  // most cap, and a count handed in through the device entries is clamped
+  // to [0, cap] so that no sweep reads past the checkpoint arrays.
+  __device__ __forceinline__ int count(size_t c) const { return min(max(n[c], 0), cap); }
 };
 
 template <int N>
@@ -584,7 +588,7 @@ __global__ void __launch_bounds__(kBlock, 2) integrate_replay_kernel(LaunchArgs 
     load_state<Mech>(a.conc, c, n, S);
     load_rates<Mech>(a, c, 0, S);
     auto k = [&](int r) { return S[Mech::KT + r]; };
-    const int cnt = ck.n[c];
+    const int cnt = ck.count(c);
     for (int s = 0; s < cnt; ++s) {
       int st = 0;
       (void)Mech::attempt(S, k, ck.h[(size_t)s * n + c], st);
@@ -620,7 +624,7 @@ __global__ void __launch_bounds__(kBlock, 2) adjoint_kernel(AdjointArgs a, Check
 #pragma unroll 4
     for (int i = 0; i < Mech::NV; ++i) S[Mech::LAM + i] = a.lam[c + n * Mech::var_phys(i)];
     auto k = [&](int r) { return S[Mech::KT + r]; };
-    for (int s = ck.n[c] - 1; s >= 0; --s) {
+    for (int s = ck.count(c) - 1; s >= 0; --s) {
 #pragma unroll 4
       for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] = ck.y[((size_t)s * Mech::NV + i) * n + c];
       const double h = ck.h[(size_t)s * n + c];
@@ -662,7 +666,7 @@ __global__ void __launch_bounds__(kBlock, 2) tangent_kernel(TangentArgs a, Check
 #pragma unroll 4
     for (int i = 0; i < Mech::NV; ++i) S[Mech::DYT + i] = a.dconc0[c + n * Mech::var_phys(i)];
     auto k = [&](int r) { return S[Mech::KT + r]; };
-    const int cnt = ck.n[c];
+    const int cnt = ck.count(c);
     for (int s = 0; s < cnt; ++s) {
 #pragma unroll 4
       for (int i = 0; i < Mech::NV; ++i) S[Mech::Y + i] = ck.y[((size_t)s * Mech::NV + i) * n + c];

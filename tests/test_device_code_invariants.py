@@ -13,7 +13,9 @@ code (csrc/solver.cuh, csrc/mkpp_device.cuh):
 * every slot a program word addresses (the cooperative stage programs, the
   table-driven adjoint and evaluation, the tangent program) lies inside the store the
   kernel gives that program, checked here from the emitted tables instead
-  of by bounds checks on the device.
+  of by bounds checks on the device;
+* the checkpoint sweeps clamp the caller's recorded-step counts to the
+  checkpoint capacity.
 """
 import re
 from pathlib import Path
@@ -122,3 +124,15 @@ def test_program_slots_lie_inside_their_stores(path):
     body = text[text.index("static void tlm_step("):]
     body = body[:body.index("\n  }\n")]
     assert all(int(i) < tlm for i in re.findall(r"S\[(\d+)\] =", body))
+
+
+def test_checkpoint_sweeps_read_clamped_counts():
+    """The replay, adjoint and tangent sweeps read a cell's recorded-step
+    count through CheckpointArgs::count (clamped to [0, cap]), since the
+    device entries take the count array from the caller; only the forward
+    that records the steps writes n[c] itself."""
+    code = _code(HANDWRITTEN[0])
+    reads = re.findall(r"ck\.n\[c\][^\n;]*", code)
+    assert reads == ["ck.n[c] = cnt"]
+    assert len(re.findall(r"ck\.count\(c\)", code)) == 3
+    assert re.search(r"int count\(size_t c\) const \{ return min\(max\(n\[c\], 0\), cap\); \}", code)
