@@ -30,7 +30,9 @@
 //   numerical failure), not only the non-finite inputs the reference records;
 //   team_size is accepted and unused (the GPU kernels size their own grids).
 //
-// Header-only, C++17; link with -ldl.
+// Header-only, C++17; link with -ldl.  With the CUDA toolkit's include
+// directory on the path, the batched dispatch opens the reference's NVTX
+// range MKPP_Batched_Team_Dispatch_<name>.
 #pragma once
 
 #include <dlfcn.h>
@@ -50,8 +52,39 @@
 
 #include "mkpp.h"
 
+// NVTX3 is header-only and ships with the CUDA toolkit; with its include
+// directory on the path the batched dispatch opens an NVTX range, otherwise
+// the range is a no-op.
+#if defined(__has_include)
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define MKPP_HOST_NVTX 1
+#endif
+#endif
+
 namespace mkpp {
 namespace host {
+
+// A named profiler range over a scope, as the reference's Kokkos profiling
+// regions (Kokkos::Profiling::ScopedRegion).  Without a profiler attached,
+// NVTX calls do nothing.
+class TraceRange {
+ public:
+  explicit TraceRange(const std::string& name) {
+#ifdef MKPP_HOST_NVTX
+    nvtxRangePushA(name.c_str());
+#else
+    (void)name;
+#endif
+  }
+  ~TraceRange() {
+#ifdef MKPP_HOST_NVTX
+    nvtxRangePop();
+#endif
+  }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 
 enum CellErrorCode : int {
   SUCCESS = MKPP_CELL_SUCCESS,
@@ -335,6 +368,8 @@ void execute_mechanism_steps_batched(const std::string& name, double* state, std
     std::cerr << err << std::endl;
     throw std::runtime_error(err);
   }
+  // The reference's region name (dispatcher.hpp:335).
+  const TraceRange range("MKPP_Batched_Team_Dispatch_" + name);
   HostExecutionParams p;
   p.dt = dt;
   p.steps = steps;

@@ -35,6 +35,11 @@ if(NOT TARGET mkpp_gb300::registry)
   target_compile_definitions(mkpp_gb300_registry INTERFACE "MKPP_GB300_LIB_DIR=\"${MKPP_GB300_LIB_DIR}\"")
   target_compile_features(mkpp_gb300_registry INTERFACE cxx_std_17)
   target_link_libraries(mkpp_gb300_registry INTERFACE ${CMAKE_DL_LIBS})
+  # Header-only NVTX3 from the CUDA toolkit: the batched dispatch's profiler range.
+  find_package(CUDAToolkit QUIET)
+  if(TARGET CUDA::nvtx3)
+    target_link_libraries(mkpp_gb300_registry INTERFACE CUDA::nvtx3)
+  endif()
   add_library(mkpp_gb300::registry ALIAS mkpp_gb300_registry)
 endif()
 

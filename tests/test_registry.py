@@ -143,3 +143,29 @@ def test_batched_path_isolates_non_finite_cell(checker, tmp_path):
     finally:
         ctx.close()
     assert np.array_equal(got, ref, equal_nan=True)
+
+
+def test_registry_builds_with_nvtx_ranges(tmp_path):
+    """With the CUDA toolkit's include directory on the path, the header opens
+    the reference's NVTX range MKPP_Batched_Team_Dispatch_<name>
+    (dispatcher.hpp:335) around the batched dispatch; it still builds without
+    warnings and finds the libraries."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from mkpp_gb300 import build
+
+    try:
+        cuda_inc = Path(build.nvcc()).resolve().parent.parent / "include"
+        build.build(("chapman",))
+    except RuntimeError as e:  # no nvcc
+        pytest.skip(str(e))
+    if not (cuda_inc / "nvtx3" / "nvToolsExt.h").exists():
+        pytest.skip("no NVTX3 headers in the CUDA toolkit")
+    header = (ROOT / "include" / "mkpp_host" / "mechanism_manager.hpp").read_text()
+    assert 'TraceRange range("MKPP_Batched_Team_Dispatch_" + name)' in header
+    exe = tmp_path / "registry_check_nvtx"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
+                    f"-I{cuda_inc}", str(ROOT / "tests" / "registry" / "registry_check.cpp"), "-ldl", "-o", str(exe)],
+                   check=True)
+    out = _run(exe, "list")
+    assert out.returncode == 0 and "chapman" in out.stdout.split(), out.stderr
