@@ -22,7 +22,11 @@ Workloads (cells, host steps x dt):
   phi_c ~ U[0, 2 pi) (diurnal cosine of the solar zenith angle) and per-slot
   maxima Jmax_r log-uniform in [1e-6, 1e-2] 1/s (NO2 -> 8e-3 1/s).
 * ``ts1``           1048576 cells, 6 x 600 s, mol/m3 units (molec/cm3 / 6.02214076e17),
-  40 % night, 30 % clean (NOx x 0.01), 30 % polluted (NOx x 100).
+  40 % night, 30 % clean (NOx x 0.01), 30 % polluted (NOx x 100).  Species
+  log-uniform in [1e-2, 1e12] molec/cm3, photolysis as ``saprc99``, the user
+  and heterogeneous rate slots from the reference's TS1 benchmark inputs.
+  Its plan's atol is 1 molec/cm3 expressed in mol/m3 (1.66e-18), rtol 1e-3:
+  the tolerances of the other workloads in TS1's units.
 
 Further mechanisms the reference ships (no benchmark configuration; parity
 cases only):
@@ -193,10 +197,31 @@ def ts1(ncells: int = 1048576, seed: int = SEED) -> Workload:
     phase[kind == 0] = np.pi                     # night cells: sun below horizon all run
     jmax = _jmax(raw, rng)
     param = np.zeros((raw["num_rate_parameters"], ncells))
+    # The slots after the photolysis rates are user and heterogeneous rate
+    # constants addressed by reaction index; every cell takes the values of
+    # the reference's TS1 benchmark inputs.
+    nph = raw["num_photolysis"]
+    param[nph:] = ts1_user_rates(raw)[nph:, None]
     w = Workload("ts1", "ts1", conc, T, p, (M * to_mol_m3), np.full(ncells, 0.5), param, 600.0, 6,
                  phase=phase, jmax=jmax, extra={"kind": kind})
     w.param = w.param_at(0)
     return w
+
+
+def ts1_user_rates(raw=None) -> np.ndarray:
+    """TS1's runtime parameter row of the reference's native benchmark run
+    (``benchmarks/solver_comparison/runners/mkpp/ts1_binding_data.hpp:246``,
+    kept as the ``parameters`` of ``tests/golden/ts1_kokkos_2x300.json``).
+    Slots 361-373, 499 and 529-546 are nonzero there: uptake on aerosol and
+    heterogeneous halogen reactions, in 1/s or m3/(mol s)."""
+    import json
+    from pathlib import Path
+
+    raw = raw or load_raw("ts1")
+    path = Path(__file__).resolve().parent.parent / "tests" / "golden" / "ts1_kokkos_2x300.json"
+    row = np.asarray(json.loads(path.read_text())["parameters"], dtype=np.float64)
+    assert row.shape == (raw["num_rate_parameters"],)
+    return row
 
 
 def _photolysis_slot(raw, species):

@@ -11,8 +11,10 @@ Here:
   cells both finish.  Six rate constants of the shipped TS1 reach 1e29-1e41
   1/s (Troe k0 evaluated as A exp(+C/T)); as for SAPRC99 they are moderated
   to 1e3 so that the comparison measures the arithmetic rather than the
-  conditioning.  Even then ~20% of the synthetic cells end non-finite on
-  both sides;
+  conditioning.  With them moderated, the oracle against itself under a
+  one-ulp change of every rate constant moves by at most 1e-11 on these
+  cells (atol 1 molec/cm3 in TS1's mol/m3), so 1e-9 is a gate on the
+  arithmetic;
 * the evaluation entries, table-driven too (one sequential program per
   cell for the partials, W and F), against the oracle.
 """
@@ -70,7 +72,7 @@ def test_ts1_forced_step_sequence_parity(ts1_lib):
     rep = o.integrate(w.conc.copy(), w.dt, k=k_ref, dk=dk, temp=w.temp, rho=w.rho, rh=w.rh, param=w.param,
                       replay=(log["log_h"].cpu().numpy(), log["log_acc"].cpu().numpy(), ln))
     ok &= rep["status"] == 0
-    assert ok.mean() > 0.6
+    assert ok.mean() > 0.9
     got, ref = conc.cpu().numpy()[:, ok], rep["conc"][:, ok]
     atol = np.array(o.raw["atol"])[:, None]
     assert (np.abs(got - ref) / (np.abs(ref) + atol)).max() <= 1e-9
