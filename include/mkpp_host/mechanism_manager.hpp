@@ -165,7 +165,15 @@ struct Library {
   int (*integrate)(mkpp_handle_t, double){nullptr};
   int (*cell_stats)(mkpp_handle_t, int*, int*, int*){nullptr};
   int (*last_error)(mkpp_handle_t, char*, size_t){nullptr};
+  int (*set_seed)(mkpp_handle_t, double){nullptr};
+  int (*evaluate_rates)(mkpp_handle_t, double*){nullptr};
+  int (*evaluate_jacobian)(mkpp_handle_t, double*){nullptr};
+  int (*jacobian_vector)(mkpp_handle_t, const double*, double*){nullptr};
+  int (*jacobian_transpose_vector)(mkpp_handle_t, const double*, double*){nullptr};
   std::map<std::size_t, mkpp_handle_t> handles;  // one per cell count, kept for the process
+  // Handles of the per-cell SolverKernels entry points
+  // (mkpp_gb300/solver_kernels.hpp), kept apart because those set the seed.
+  std::map<std::size_t, mkpp_handle_t> kernel_handles;
 };
 
 inline std::string library_dir() {
@@ -235,6 +243,11 @@ inline Library& library(const std::string& name) {
   bind(*lib, lib->integrate, "mkpp_integrate");
   bind(*lib, lib->cell_stats, "mkpp_get_cell_stats");
   bind(*lib, lib->last_error, "mkpp_get_last_error");
+  bind(*lib, lib->set_seed, "mkpp_set_initial_step_seed");
+  bind(*lib, lib->evaluate_rates, "mkpp_evaluate_rates");
+  bind(*lib, lib->evaluate_jacobian, "mkpp_evaluate_jacobian");
+  bind(*lib, lib->jacobian_vector, "mkpp_evaluate_jacobian_vector");
+  bind(*lib, lib->jacobian_transpose_vector, "mkpp_evaluate_jacobian_transpose_vector");
   lib->sizes(&lib->num_species, &lib->num_variable, &lib->num_reactions, &lib->num_parameters, &lib->num_lu);
   (*libs)[name] = lib;
   return *lib;
@@ -247,6 +260,22 @@ inline Library& library(const std::string& name) {
                            : "FATAL ERROR: " + std::string(what) + " returned " + std::to_string(rc) + " for " + lib.name;
   std::cerr << err << std::endl;
   throw std::runtime_error(err);
+}
+
+// The library's handle for n cells from `pool` (lib.handles unless given),
+// created and initialised on first use (call with lock() held).
+inline mkpp_handle_t handle(Library& lib, std::size_t n, std::map<std::size_t, mkpp_handle_t>* pool = nullptr) {
+  mkpp_handle_t& h = (pool ? *pool : lib.handles)[n];
+  if (!h) {
+    int rc = lib.create(&h, n);
+    if (rc != MKPP_SUCCESS) {
+      h = nullptr;
+      fail(lib, nullptr, rc, "mkpp_create_handle");
+    }
+    rc = lib.initialize(h);
+    if (rc != MKPP_SUCCESS) fail(lib, h, rc, "mkpp_initialize");
+  }
+  return h;
 }
 
 }  // namespace detail
@@ -303,18 +332,8 @@ class MechanismRegistry {
       }
     }
 
-    mkpp_handle_t& h = lib.handles[n];
-    int rc = MKPP_SUCCESS;
-    if (!h) {
-      rc = lib.create(&h, n);
-      if (rc != MKPP_SUCCESS) {
-        h = nullptr;
-        detail::fail(lib, nullptr, rc, "mkpp_create_handle");
-      }
-      rc = lib.initialize(h);
-      if (rc != MKPP_SUCCESS) detail::fail(lib, h, rc, "mkpp_initialize");
-    }
-    rc = lib.set_state(h, state, temp.data(), pressure.data(), rho.data());
+    mkpp_handle_t h = detail::handle(lib, n);
+    int rc = lib.set_state(h, state, temp.data(), pressure.data(), rho.data());
     if (rc != MKPP_SUCCESS) detail::fail(lib, h, rc, "mkpp_set_state_ptrs");
     rc = lib.set_aerosol(h, rh.data(), nullptr);
     if (rc != MKPP_SUCCESS) detail::fail(lib, h, rc, "mkpp_set_aerosol_ptrs");

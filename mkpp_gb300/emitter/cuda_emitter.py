@@ -1499,6 +1499,66 @@ def emit_host_header(plan) -> str:
 """
 
 
+def emit_solver_kernels_header(plan) -> str:
+    """generated/host_api/<m>/<m>.hpp: the reference's generated C++ API of
+    one mechanism (src/mkpp/templates/header.j2:70-80,127-203): namespace
+    mkpp::generated::<m> with enum Species and SolverKernels<DeviceType>,
+    here include/mkpp_gb300/solver_kernels.hpp bound to libmkpp_<m>.so."""
+    raw = plan.raw
+    name = plan.name
+    ns = len(raw["species"])
+
+    def lits(xs):
+        return ", ".join(repr(float(x)) for x in xs)
+
+    species = ",\n".join(f"    {sp} = {i}" for i, sp in enumerate(raw["species"]))
+    pattern = ", ".join(f"{{{i}, {j}}}" for i, j in raw["jacobian_entries"])
+    flag = lambda b: "true" if b else "false"  # noqa: E731
+    return f"""// {name}.hpp of the {name} library (libmkpp_{name}.so), generated from its
+// plan: the reference's generated C++ solver API for this mechanism
+// (src/mkpp/templates/header.j2:70-80,127-203), namespace
+// mkpp::generated::{name} with enum Species and SolverKernels<DeviceType>.
+// The members and their execution are described in
+// include/mkpp_gb300/solver_kernels.hpp.
+#pragma once
+
+#include "../../../../include/mkpp_gb300/solver_kernels.hpp"
+
+namespace mkpp {{
+namespace generated {{
+namespace {name} {{
+
+enum Species : int {{
+{species}
+}};
+
+struct MechanismConstants {{
+  static constexpr const char* NAME = "{name}";
+  static constexpr int NUM_SPECIES = {ns};
+  static constexpr int NUM_RUNTIME_PARAMETERS = {raw["num_rate_parameters"]};
+  static constexpr int NUM_PHOTOLYSIS = {raw["num_photolysis"]};
+  static constexpr int NUM_REACTIONS = {raw["num_reactions"]};
+  static constexpr bool SUPPORTS_RUNTIME_ENVIRONMENT = {flag(raw["runtime_environment"])};
+  static constexpr bool HAS_CLOUD_GATED = {flag(raw["cloud_gated"])};
+  static constexpr double ENV_TEMPERATURE = {float(raw["environment_temperature"])!r};
+  static constexpr double ENV_AIR_DENSITY = {float(raw["environment_air_density"])!r};
+  static constexpr double INITIAL_STEP_SEED = {float(raw["initial_step_seed"])!r};
+  static constexpr double atol[NUM_SPECIES] = {{{lits(raw["atol"])}}};
+  static constexpr double rtol[NUM_SPECIES] = {{{lits(raw["rtol"])}}};
+  // (row, column) of the Jacobian entries compute_jacobian writes
+  static constexpr int NUM_JACOBIAN_ENTRIES = {len(raw["jacobian_entries"])};
+  static constexpr int jacobian_pattern[NUM_JACOBIAN_ENTRIES][2] = {{{pattern}}};
+}};
+
+template <class DeviceType>
+struct SolverKernels : ::mkpp_gb300::SolverKernelsBase<MechanismConstants, DeviceType> {{}};
+
+}}  // namespace {name}
+}}  // namespace generated
+}}  // namespace mkpp
+"""
+
+
 def _write_if_changed(path: Path, text: str) -> None:
     path.parent.mkdir(parents=True, exist_ok=True)
     if not path.exists() or path.read_text() != text:
@@ -1510,6 +1570,7 @@ def write(name: str, out_dir: Path = GEN_DIR) -> Path:
     path = out_dir / f"{name}.cuh"
     _write_if_changed(path, emit_mechanism(plan))
     _write_if_changed(out_dir / "host_api" / name / "mkpp.h", emit_host_header(plan))
+    _write_if_changed(out_dir / "host_api" / name / f"{name}.hpp", emit_solver_kernels_header(plan))
     return path
 
 

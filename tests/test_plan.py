@@ -67,6 +67,8 @@ def test_generated_header_is_current(mech):
     assert path.read_text() == text, "regenerate with python -m mkpp_gb300.emitter.cuda_emitter"
     host = cuda_emitter.GEN_DIR / "host_api" / mech / "mkpp.h"
     assert host.read_text() == cuda_emitter.emit_host_header(plan)
+    kernels = cuda_emitter.GEN_DIR / "host_api" / mech / f"{mech}.hpp"
+    assert kernels.read_text() == cuda_emitter.emit_solver_kernels_header(plan)
 
 
 def test_tableaux_match_reference_coefficients():
@@ -91,3 +93,5 @@ def test_tolerance_variant_differs_only_in_name_and_tolerances():
     assert (cuda_emitter.GEN_DIR / "chapman_shipped.cuh").read_text() == cuda_emitter.emit_mechanism(plan)
     assert ((cuda_emitter.GEN_DIR / "host_api" / "chapman_shipped" / "mkpp.h").read_text()
             == cuda_emitter.emit_host_header(plan))
+    assert ((cuda_emitter.GEN_DIR / "host_api" / "chapman_shipped" / "chapman_shipped.hpp").read_text()
+            == cuda_emitter.emit_solver_kernels_header(plan))
