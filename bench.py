@@ -33,6 +33,12 @@ import threading
 import time
 from pathlib import Path
 
+# Thread placement of the CPU legs (the reference solver's OpenMP loop):
+# spread over all cores, one thread per core, as the reference's benchmark
+# recipe runs it.  Read once, when the OpenMP runtime starts.
+os.environ.setdefault("OMP_PROC_BIND", "spread")
+os.environ.setdefault("OMP_PLACES", "cores")
+
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
@@ -65,7 +71,9 @@ def parse():
     ap.add_argument("--workload", default="saprc99")
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--host-steps", type=int, default=None)
-    ap.add_argument("--cpu-cells", type=int, default=256, help="cells in the bounded CPU sample")
+    ap.add_argument("--cpu-cells", type=int, default=None,
+                    help="cells in the bounded CPU sample (default max(4096, 64 x threads): every thread gets "
+                         "at least one of the reference's 64-cell chunks per host step)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--max-attempts", type=int, default=20000)
@@ -173,27 +181,45 @@ def max_over_ranks(x: float, world: int) -> float:
 
 
 # ---------------------------------------------------------------------------
-def cpu_reference_sample(w, cells: int, host_steps: int, threads: int):
-    """Time the CPU implementation on the first `cells` cells of the workload."""
-    sub = w.subset(cells)
+def cpu_sample_cells(args, threads: int) -> int:
+    """Cells of the CPU sample: at least 4096, and at least one 64-cell chunk
+    of the reference's static OpenMP schedule per thread."""
+    return args.cpu_cells or max(4096, 64 * threads)
+
+
+def cpu_runner(mechanism: str):
+    """The reference's own CPU solver built here (kind "reference"), else the
+    oracle port (kind "port")."""
     try:
         from oracle import ref_build
 
-        ref = ref_build.load(sub.mechanism)
+        ref = ref_build.load(mechanism)
     except Exception:
         ref = None
     if ref is not None:
-        kind, runner = "reference", ref
-    else:
-        from oracle.oracle import Oracle
+        return "reference", ref
+    from oracle.oracle import Oracle
 
-        kind, runner = "port", Oracle(sub.mechanism)
-    conc = sub.conc.copy()
+    return "port", Oracle(mechanism)
+
+
+def cpu_integrate(runner, sub, conc, first: int, last: int, threads: int) -> float:
+    """Host steps [first, last) of every cell of `sub`, in place on conc;
+    returns the seconds.  One OpenMP parallel region per host step, as the
+    reference's host loop calls its dispatcher once per host step."""
     t0 = time.perf_counter()
-    for s in range(host_steps):
+    for s in range(first, last):
         runner.integrate(conc, sub.dt, temp=sub.temp, rho=sub.rho, rh=sub.rh, param=sub.param_at(s),
                          nthreads=threads)
-    el = time.perf_counter() - t0
+    return time.perf_counter() - t0
+
+
+def cpu_reference_sample(w, cells: int, host_steps: int, threads: int):
+    """Time the CPU implementation on the first `cells` cells of the workload,
+    all host steps."""
+    sub = w.subset(cells)
+    kind, runner = cpu_runner(sub.mechanism)
+    el = cpu_integrate(runner, sub, sub.conc.copy(), 0, host_steps, threads)
     return kind, cells * host_steps / el, el
 
 
@@ -205,21 +231,40 @@ def run_reference(args, world, rank):
     w = workloads.make(args.workload, args.cells)
     hs = args.host_steps or w.host_steps
     threads = os.cpu_count() or 1
-    vals = []
-    kind = "port"
-    for i in range(args.warmup + args.steps):
-        kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
-        if i >= args.warmup:
-            vals.append((v, el))
-    value = statistics.median(v for v, _ in vals)
-    ms = statistics.median(el for _, el in vals) * 1e3
-    sample = f"first {args.cpu_cells} of {w.ncells} cells x {hs} host steps of {w.dt:g} s"
+    cells = min(cpu_sample_cells(args, threads), w.ncells)
+    kind, runner = cpu_runner(w.mechanism)
+    # Warm-up steps: one host step of one 64-cell chunk per thread.
+    warm = w.subset(min(64 * threads, w.ncells))
+    for _ in range(args.warmup):
+        cpu_integrate(runner, warm, warm.conc.copy(), 0, 1, threads)
+    # Timed steps: together they integrate one whole window (all host steps)
+    # of the sample, step i taking host steps [hs i / K, hs (i + 1) / K), so
+    # the run stays bounded whatever K is while the sample keeps the cost mix
+    # of the whole window (the first host step is the stiffest).  With more
+    # steps than host steps, windows repeat from the initial state.
+    sub = w.subset(cells)
+    windows = -(-args.steps // hs)
+    passes = windows * hs
+    conc = sub.conc.copy()
+    total = 0.0
+    for i in range(args.steps):
+        for x in range(passes * i // args.steps, passes * (i + 1) // args.steps):
+            if x % hs == 0:
+                conc = sub.conc.copy()
+            total += cpu_integrate(runner, sub, conc, x % hs, x % hs + 1, threads)
+    value = cells * passes / total
+    ms = total / args.steps * 1e3
+    sample = (f"first {cells} of {w.ncells} cells x {hs} host steps of {w.dt:g} s"
+              + (f" ({windows} windows)" if windows > 1 else "") + f", split over the {args.steps} timed steps; "
+              f"OpenMP static chunks of 64 cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+              f"OMP_PLACES={os.environ.get('OMP_PLACES')}")
     line = {
         "impl": "reference", "metric": metric_for(w.mechanism), "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(w, hs),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+                         "seconds": total},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -386,7 +431,10 @@ def main():
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
                  "attempts_per_cell_window_pct": {q: float(np.percentile(att, q)) for q in (50, 90, 99, 100)},
-                 "cell_status_counts": np.bincount(st_h, minlength=5).tolist()},
+                 "cell_status_counts": np.bincount(st_h, minlength=5).tolist(),
+                 # value counting only the cells that end finite (status 4 is
+                 # a non-finite result, as the oracle gives for the same cells)
+                 "value_finite_cells_only": float((st_h != 4).sum()) * hs / (el_ms * 1e-3)},
         "roofline": {
             "bound": "fp64", "achieved": achieved, "peak": best, "unit": "TFLOP/s",
             "frac": (achieved / best) if achieved and best else None,
@@ -549,11 +597,20 @@ def main():
     if rank == 0 and world == 1:
         with optional_section(result, "cpu_baseline", True):
             threads = os.cpu_count() or 1
-            kind, v, el = cpu_reference_sample(w, args.cpu_cells, hs, threads)
+            cells = min(cpu_sample_cells(args, threads), n)
+            kind, v, el = cpu_reference_sample(w, cells, hs, threads)
             log(f"cpu baseline ({kind}): {el:.1f} s")
-            result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                                      "sample": f"first {args.cpu_cells} of {n} cells x {hs} host steps of {w.dt:g} s",
-                                      "seconds": el}
+            # The sample's cost mix against the whole run's, from the GPU's
+            # attempt counters on the same cells (the CPU solver runs the
+            # same controller, so it makes the same attempts up to round-off).
+            result["cpu_baseline"] = {
+                "value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                "sample": f"first {cells} of {n} cells x {hs} host steps of {w.dt:g} s, OpenMP static chunks of 64 "
+                          f"cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+                          f"OMP_PLACES={os.environ.get('OMP_PLACES')}",
+                "seconds": el,
+                "attempts_per_cell_solve_sample": float(att[:cells].sum()) / (cells * hs),
+                "attempts_per_cell_solve_run": attempts / (n * hs)}
 
     if rank == 0:
         print(json.dumps(result), flush=True)
