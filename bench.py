@@ -88,6 +88,14 @@ def parse():
                     help="tail parking threshold in attempts for every integrate launch (mkpp_set_tail_parking; 0 off)")
     ap.add_argument("--e2e-cost-order", type=int, default=0,
                     help="e2e handle hands out the previous call's most expensive cells first (mkpp_set_cost_order)")
+    ap.add_argument("--bulk-cells", type=int, default=77824,
+                    help="cells of the bulk-rate section (every cell capped at --bulk-attempts attempts)")
+    ap.add_argument("--bulk-attempts", type=int, default=20)
+    ap.add_argument("--bulk-defer", type=int, default=0,
+                    help="park each cell for the warp-cooperative kernel after this many attempts (0: never); "
+                         "1 with few cells measures the cooperative kernel's attempt latency")
+    ap.add_argument("--bulk-only", action="store_true",
+                    help="run only the bulk-rate section (a small case for profilers) and print its JSON")
     return ap.parse_args()
 
 
@@ -181,6 +189,47 @@ def max_over_ranks(x: float, world: int) -> float:
 
 
 # ---------------------------------------------------------------------------
+def bulk_rate(mechanism: str, cells: int, attempts: int, stream=None, defer: int = 0) -> dict:
+    """Attempt throughput of the persistent kernel with every lane busy: the
+    first `cells` cells of the workload (first host step) with every cell
+    capped at `attempts` attempts, so no cell finishes early and there is no
+    tail; nothing is parked unless `defer` > 0, which parks every cell after
+    that many attempts (this sets the process's parking threshold, so it runs
+    last).  Two launches, the second timed with CUDA events on the
+    launching stream.  Explains the window's roofline fraction: the gap
+    between the two is the tail."""
+    import torch
+
+    from mkpp_gb300 import workloads
+    from mkpp_gb300.api import DeviceSolver
+    from mkpp_gb300.emitter.plan import flops_per_attempt, load
+
+    w = workloads.make(mechanism, cells)
+    s = DeviceSolver(mechanism)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    conc0 = d(w.conc)
+    stream = stream or torch.cuda.current_stream()
+    with torch.cuda.stream(stream):
+        ktab, status = s.rate_constants(conc0, d(w.temp), d(w.rho), d(w.rh), None, d(w.param))
+        s.set_tuning(defer_after=defer)
+        for rep in range(2):
+            conc = conc0.clone()
+            st = status.clone()
+            acc = torch.zeros(cells, dtype=torch.int32, device="cuda")
+            rej = torch.zeros_like(acc)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.integrate_k(conc, ktab, w.dt, max_attempts=attempts, mode="persistent", status=st, accepted=acc,
+                          rejected=rej)
+            b.record(stream)
+            stream.synchronize()
+    att = int((acc + rej).sum())
+    ms = a.elapsed_time(b)
+    flops = flops_per_attempt(load(mechanism))["total"]
+    return {"cells": cells, "attempt_cap": attempts, "defer_after": defer, "attempts": att, "ms": ms,
+            "attempts_per_s": att / (ms * 1e-3), "tflops": att * flops / (ms * 1e-3) / 1e12}
+
+
 def cpu_sample_cells(args, threads: int) -> int:
     """Cells of the CPU sample: at least 4096, and at least one 64-cell chunk
     of the reference's static OpenMP schedule per thread."""
@@ -298,6 +347,10 @@ def main():
     from mkpp_gb300.emitter.plan import flops_per_attempt, load, load_raw
 
     torch.cuda.set_device(local)
+    if args.bulk_only:
+        print(json.dumps({"bulk": bulk_rate(args.workload, args.bulk_cells, args.bulk_attempts,
+                                            defer=args.bulk_defer)}), flush=True)
+        return
     dev = torch.device("cuda", local)
     from mkpp_gb300 import shard
 
@@ -611,6 +664,13 @@ def main():
                 "seconds": el,
                 "attempts_per_cell_solve_sample": float(att[:cells].sum()) / (cells * hs),
                 "attempts_per_cell_solve_run": attempts / (n * hs)}
+
+    if rank == 0 and world == 1:
+        with optional_section(result, "bulk", True):
+            b = bulk_rate(w.mechanism, min(args.bulk_cells, n), args.bulk_attempts, stream)
+            b["frac_of_fp64_peak"] = b["tflops"] / best if best else None
+            result["bulk"] = b
+            log(f"bulk: {b['tflops']:.3f} TFLOP/s with every lane busy")
 
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -5,7 +5,7 @@ into the repository):
 
 1. Regenerate the reference's Kokkos C++ solver headers for a mechanism with
    the reference's own compiler pipeline (the steps of ``run_compiler``,
-   src/mkpp/cli.py:155-346, called directly), unchanged, with the benchmark tolerances (rtol 1e-3, atol 1) from an
+   src/mkpp/cli.py:155-346, called directly), unchanged, with the mechanism plan's tolerances (rtol 1e-3, atol 1 molec/cm3) from an
    environment file, into ``oracle/_ref/gen/<mech>/`` (git-ignored).
 2. Compile ``oracle/ref_driver.cpp`` (a small C driver of this project that
    calls the unmodified ``SolverKernels<D>::integrate()`` per cell under
@@ -35,9 +35,23 @@ HERE = Path(__file__).resolve().parent
 REF = HERE / "_ref"
 GEN = REF / "gen"
 MECHS = ("chapman", "small_strato", "saprc99")
+# Generated wherever the reference is present but compiled on demand
+# (ensure()): TS1's solver takes minutes to compile.
+ON_DEMAND = ("ts1",)
 # Further shipped mechanisms, built on demand by the parity tests (ensure()).
 EXTRA_MECHS = ("saprc99_mini", "saprcnov")
-DEFAULT_REFERENCE = "/root/reference"
+# The reference checkout this recipe reads (MKPP_REFERENCE overrides it).
+DEFAULT_REFERENCE = os.environ.get("MKPP_REFERENCE", "/root/reference")
+
+
+def _tolerances(mech: str) -> tuple[float, float]:
+    """(rtol, atol) of the mechanism's plan: the reference solver is
+    regenerated at the tolerances the GPU library runs (rtol 1e-3 and atol 1
+    molec/cm3, which for TS1's mol/m3 is 1.66e-18)."""
+    from mkpp_gb300.emitter.plan import load_raw
+
+    raw = load_raw(mech)
+    return float(raw["rtol"][0]), float(raw["atol"][0])
 
 
 def _yaml_stub():
@@ -68,8 +82,9 @@ def generate(mech: str, reference: str = DEFAULT_REFERENCE, host_api: bool = Fal
         return out
     out.mkdir(parents=True, exist_ok=True)
     env = out / "env.json"
+    rtol, atol = _tolerances(mech)
     env.write_text(json.dumps({"environment": {"temperature": 298.15, "air_density": 2.46e19},
-                               "solver": {"rtol": 1e-3, "atol": 1.0}}))
+                               "solver": {"rtol": rtol, "atol": atol}}))
     code = (
         "import sys; sys.dont_write_bytecode = True; "
         f"sys.path.insert(0, {str(HERE.parent)!r}); from oracle.ref_build import _yaml_stub; _yaml_stub(); "
@@ -152,6 +167,9 @@ def ensure(mech: str, reference: str = DEFAULT_REFERENCE):
 
 def build_if_available(reference: str = DEFAULT_REFERENCE) -> list[Path]:
     built = []
+    if Path(reference).exists():
+        for mech in ON_DEMAND:
+            generate(mech, reference)
     for mech in MECHS:
         if Path(reference).exists():
             generate(mech, reference)
