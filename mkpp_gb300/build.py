@@ -25,10 +25,13 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Libraries build() makes by default.  chapman_shipped is Chapman at the
 # shipped generated header's tolerances (rtol 1e-6, atol 1e-3), for the
-# reference's native-run golden output.  saprcnov (96 species, as large as
-# SAPRC99 to compile, no benchmark configuration) is built on request:
-# build(("saprcnov",)).
-DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99", "ts1", "saprc99_mini", "chapman_shipped")
+# reference's native-run golden output; chapman_rodas3 and
+# small_strato_rodas3 are those mechanisms with the RODAS-3 tableau
+# (src/mkpp/rosenbrock.py:71-82) instead of ROS-3.  saprcnov (96 species, as
+# large as SAPRC99 to compile, no benchmark configuration) is built on
+# request: build(("saprcnov",)).
+DEFAULT_MECHANISMS = ("chapman", "small_strato", "saprc99", "ts1", "saprc99_mini", "chapman_shipped",
+                      "chapman_rodas3", "small_strato_rodas3")
 
 
 def nvcc() -> str:

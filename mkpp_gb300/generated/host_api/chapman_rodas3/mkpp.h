@@ -1,0 +1,18 @@
+/*
+ * mkpp.h of the chapman_rodas3 library (libmkpp_chapman_rodas3.so), generated from its plan.
+ * The C ABI of include/mkpp.h plus the mechanism's sizes, as the header the
+ * reference generates per mechanism defines them
+ * (src/mkpp/templates/host_api/mkpp.h.j2:29-33).  A host model built against
+ * that header puts this directory on its include path instead.
+ */
+#ifndef MKPP_GB300_CHAPMAN_RODAS3_MKPP_H
+#define MKPP_GB300_CHAPMAN_RODAS3_MKPP_H
+
+#include "../../../../include/mkpp.h"
+
+#define MKPP_NUM_RATE_PARAMETERS 2
+#define MKPP_NUM_SPECIES   4
+#define MKPP_NUM_REACTIONS 4
+#define MKPP_NUM_PHOTOLYSIS 2
+
+#endif

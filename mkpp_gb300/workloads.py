@@ -281,6 +281,15 @@ BUILDERS = {"chapman": chapman, "small_strato": small_strato, "saprc99": saprc99
             "saprc99_mini": saprc99_mini, "saprcnov": saprcnov}
 
 
+# Libraries of a mechanism built with another tableau or other tolerances
+# draw that mechanism's workload.
+ALIASES = {"chapman_rodas3": "chapman", "small_strato_rodas3": "small_strato", "chapman_shipped": "chapman"}
+
+
 def make(name: str, ncells: int | None = None, seed: int = SEED) -> Workload:
-    fn = BUILDERS[name]
-    return fn(seed=seed) if ncells is None else fn(ncells, seed=seed)
+    base = ALIASES.get(name, name)
+    fn = BUILDERS[base]
+    w = fn(seed=seed) if ncells is None else fn(ncells, seed=seed)
+    if base != name:
+        w.name = w.mechanism = name
+    return w

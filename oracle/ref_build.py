@@ -36,12 +36,22 @@ REF = HERE / "_ref"
 GEN = REF / "gen"
 MECHS = ("chapman", "small_strato", "saprc99")
 # Generated wherever the reference is present but compiled on demand
-# (ensure()): TS1's solver takes minutes to compile.
+# (ensure()): TS1's solver takes a minute or more to compile.
 ON_DEMAND = ("ts1",)
 # Further shipped mechanisms, built on demand by the parity tests (ensure()).
 EXTRA_MECHS = ("saprc99_mini", "saprcnov")
 # The reference checkout this recipe reads (MKPP_REFERENCE overrides it).
 DEFAULT_REFERENCE = os.environ.get("MKPP_REFERENCE", "/root/reference")
+
+
+# Libraries that are a shipped mechanism with another tableau: name ->
+# (mechanism, the reference compiler's solver name).
+VARIANTS = {"chapman_rodas3": ("chapman", "rodas3"), "small_strato_rodas3": ("small_strato", "rodas3")}
+
+
+def _source(lib: str) -> tuple[str, str]:
+    """(mechanism, solver) the reference compiler builds library `lib` from."""
+    return VARIANTS.get(lib, (lib, "ros3"))
 
 
 def _tolerances(mech: str) -> tuple[float, float]:
@@ -77,8 +87,9 @@ def generate(mech: str, reference: str = DEFAULT_REFERENCE, host_api: bool = Fal
     """Step 1: the reference compiler writes gen/<mech>/<mech>.hpp and fragments
     (host_api: host_api/<mech>/ with its generated host API as well: mkpp.h,
     the C++ wrapper mkpp.hpp, the C ABI and the Fortran module)."""
+    src, solver = _source(mech)
     out = (REF / "host_api" / mech) if host_api else (GEN / mech)
-    if (out / ("mkpp.hpp" if host_api else f"{mech}.hpp")).exists():
+    if (out / ("mkpp.hpp" if host_api else f"{src}.hpp")).exists():
         return out
     out.mkdir(parents=True, exist_ok=True)
     env = out / "env.json"
@@ -93,7 +104,7 @@ def generate(mech: str, reference: str = DEFAULT_REFERENCE, host_api: bool = Fal
         "from mkpp.lowering import partition_reactions, prepare_adjoint_and_tlm, prepare_unified_jacobian; "
         "from mkpp.codegen import generate_headers; "
         f"env = load_environment({str(env)!r}); "
-        f"mech = load_mechanism({reference + '/mechanisms/openatmos/' + mech + '/mechanism.json'!r}); "
+        f"mech = load_mechanism({reference + '/mechanisms/openatmos/' + src + '/mechanism.json'!r}); "
         # the metadata wiring of run_compiler (src/mkpp/cli.py:223-236)
         "mech.metadata = mech.metadata or {}; "
         "mech.metadata['temperature'] = str(env.temperature); mech.metadata['air_density'] = str(env.air_density); "
@@ -101,7 +112,7 @@ def generate(mech: str, reference: str = DEFAULT_REFERENCE, host_api: bool = Fal
         "mech.metadata['rtol'] = [env.solver_rtol] * len(mech.species); "
         "b = partition_reactions(mech); mech.partition_metadata = b.get('metadata'); "
         "prepare_adjoint_and_tlm(mech); mech.sympy_metadata = prepare_unified_jacobian(mech); "
-        f"generate_headers(mech, out_dir={str(out)!r}, solver_name='ros3', generate_host_api={host_api!r})"
+        f"generate_headers(mech, out_dir={str(out)!r}, solver_name={solver!r}, generate_host_api={host_api!r})"
     )
     subprocess.run([sys.executable, "-c", code], check=True, cwd=str(out),
                    env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"))
@@ -114,15 +125,16 @@ def lib_path(mech: str) -> Path:
 
 def compile_driver(mech: str) -> Path:
     """Step 2: g++ -O3 -fopenmp the driver against the regenerated headers."""
+    base, _ = _source(mech)
     gen = GEN / mech
     out = lib_path(mech)
     src = HERE / "ref_driver.cpp"
-    if out.exists() and out.stat().st_mtime >= max(src.stat().st_mtime, (gen / f"{mech}.hpp").stat().st_mtime):
+    if out.exists() and out.stat().st_mtime >= max(src.stat().st_mtime, (gen / f"{base}.hpp").stat().st_mtime):
         return out
     tmp = out.with_suffix(f".so.tmp{os.getpid()}")
     cmd = [os.environ.get("CXX", "g++"), "-O3", "-std=c++20", "-fopenmp", "-shared", "-fPIC",
-           f"-I{HERE / 'kokkos_shim'}", f"-I{gen}", f"-DMKPP_REF_HEADER=\"{mech}.hpp\"",
-           f"-DMKPP_REF_NS=mkpp::generated::{mech}", str(src), "-o", str(tmp)]
+           f"-I{HERE / 'kokkos_shim'}", f"-I{gen}", f"-DMKPP_REF_HEADER=\"{base}.hpp\"",
+           f"-DMKPP_REF_NS=mkpp::generated::{base}", str(src), "-o", str(tmp)]
     subprocess.run(cmd, check=True)
     os.replace(tmp, out)
     return out
@@ -159,7 +171,7 @@ def ensure(mech: str, reference: str = DEFAULT_REFERENCE):
     checkout (or headers generated from it earlier) is present; else None."""
     if Path(reference).exists():
         generate(mech, reference)
-    if not (GEN / mech / f"{mech}.hpp").exists():
+    if not (GEN / mech / f"{_source(mech)[0]}.hpp").exists():
         return None
     compile_driver(mech)
     return RefSolver(mech)
@@ -168,7 +180,7 @@ def ensure(mech: str, reference: str = DEFAULT_REFERENCE):
 def build_if_available(reference: str = DEFAULT_REFERENCE) -> list[Path]:
     built = []
     if Path(reference).exists():
-        for mech in ON_DEMAND:
+        for mech in ON_DEMAND + tuple(VARIANTS):
             generate(mech, reference)
     for mech in MECHS:
         if Path(reference).exists():

@@ -26,7 +26,7 @@ def _cuda_available() -> bool:
 # allocation-free entry point last.  Other modules keep their place before them.
 GPU_ORDER = ("test_gpu_adjoint", "test_gpu_parity", "test_gpu_scale", "test_gpu_ts1", "test_gpu_tuning",
              "test_gpu_tangent", "test_gpu_mechanisms", "test_gpu_reference", "test_gpu_golden", "test_registry",
-             "test_zz_no_alloc")
+             "test_solver_kernels", "test_gpu_window_adjoint", "test_zz_no_alloc")
 
 
 def _gpu_rank(item):
@@ -49,4 +49,4 @@ def built_libs():
     """Build (if stale) and return the mechanism libraries used by GPU tests."""
     from mkpp_gb300 import build
 
-    return build.build(("chapman", "small_strato", "saprc99"))
+    return build.build(("chapman", "small_strato", "saprc99", "chapman_rodas3", "small_strato_rodas3"))

@@ -35,11 +35,11 @@ from oracle.oracle import Oracle
 
 MECHS = ["chapman", "small_strato", "saprc99"]
 # Further mechanisms the reference ships, checked for the forward step.
-EXTRA = ["saprc99_mini", "saprcnov"]
+EXTRA = ["saprc99_mini", "saprcnov", "chapman_rodas3", "small_strato_rodas3"]
 # Step sizes of the oracle comparison: cond(W) at most ~10, 1.5e5, 3e8 and
 # (TS1, where a 1 s step already changes the state by O(1)) 2e10.
 H_ORACLE = {"chapman": 1e-4, "small_strato": 1e-4, "saprc99": 1e-6, "ts1": 1.0, "saprc99_mini": 1e-6,
-            "saprcnov": 1e-6}
+            "saprcnov": 1e-6, "chapman_rodas3": 1e-4, "small_strato_rodas3": 1e-4}
 # Rate constants of the shipped mechanisms that reach 1e29-1e41 1/s (Troe k0
 # evaluated as A exp(+C/T)); moderated to 1e3 as in the GPU forced-step test.
 EXTREME = {"saprc99": (11, 32, 69), "ts1": (375, 376, 383, 394, 397, 402), "saprc99_mini": (7,),
@@ -316,7 +316,11 @@ def _column_error(a, b):
     return (np.abs(a - b).max(axis=0) / scale).max()
 
 
-@pytest.mark.parametrize("mech", MECHS + EXTRA + ["ts1"])
+ROS3 = [m for m in MECHS + EXTRA + ["ts1"] if not m.endswith("_rodas3")]
+RODAS3 = [m for m in EXTRA if m.endswith("_rodas3")]
+
+
+@pytest.mark.parametrize("mech", ROS3)
 def test_tangent_is_the_transpose_of_the_adjoint(hostsim, mech):
     """For one step, the emitted tangent (tlm_step) and adjoint
     (adjoint_step) give the same derivative: every column of d y_new/d y and
@@ -341,6 +345,96 @@ def test_tangent_is_the_transpose_of_the_adjoint(hostsim, mech):
         tl_y, tl_k, ad_y, ad_k = _jacobians(lib, mech, y, kc, h)
         assert _column_error(tl_y, ad_y) <= bound
         assert _column_error(tl_k, ad_k) <= bound
+
+
+def _step_mp(dm, y, k, h, digits=60):
+    """One step of the dense model's tableau in `digits`-digit arithmetic
+    (mpmath): the exact map the FP64 kernels round."""
+    import mpmath as mp
+
+    mp.mp.dps = digits
+    nv, nr = dm.nv, dm.nr
+    S = mp.matrix(dm.S.tolist())
+
+    def mono(yv):
+        out = [mp.mpf(1)] * nr
+        for r, e in enumerate(dm.expo):
+            for j, pw in e.items():
+                out[r] *= yv[j] ** pw
+        return out
+
+    def dmono(yv):
+        D = mp.zeros(nr, nv)
+        for r, e in enumerate(dm.expo):
+            for j, pw in e.items():
+                v = mp.mpf(pw) * yv[j] ** (pw - 1)
+                for j2, pw2 in e.items():
+                    if j2 != j:
+                        v *= yv[j2] ** pw2
+                D[r, j] = v
+        return D
+
+    def f(yv):
+        mm = mono(yv)
+        return S * mp.matrix([k[r] * mm[r] for r in range(nr)])
+
+    D = dmono(y)
+    J = S * mp.matrix([[k[r] * D[r, j] for j in range(nv)] for r in range(nr)])
+    W = mp.eye(nv) / (mp.mpf(dm.g) * h) - J
+    K, F = [], None
+    zero = mp.zeros(nv, 1)
+    for i in range(dm.st):
+        Yi = y + sum((dm.a(i, j) * K[j] for j in range(i)), zero) if i else y
+        if dm.NewF[i]:
+            F = f(Yi)
+        K.append(mp.lu_solve(W, F + sum((dm.c(i, j) / h * K[j] for j in range(i)), zero)))
+    return y + sum((dm.M[i] * K[i] for i in range(dm.st)), zero)
+
+
+@pytest.mark.parametrize("mech", RODAS3)
+def test_rodas3_derivatives_match_high_precision(hostsim, mech):
+    """RODAS-3 (4 stages, C/h coefficients up to 4/h) amplifies round-off
+    in the derivative with respect to a stiff rate constant beyond eps
+    cond(W): on small_strato at h = 1e-3 its k = 4e7 column differs between
+    tangent and adjoint by 2e-8 while cond(W) = 3.5e4.  So both are checked
+    against the exact derivative instead: central differences of the step
+    in 60-digit arithmetic (step 1e-25 relative), every column of
+    d y_new / d y and d y_new / d k to 1e-7 of its largest entry."""
+    import mpmath as mp
+
+    from oracle.adjoint_ref import DenseModel
+
+    lib = hostsim[mech]
+    plan = load(mech)
+    dm = DenseModel(mech)
+    w, o, k, _ = _case(mech, 1)
+    y = w.conc[plan.var_phys, 0]
+    kc = k[:, 0]
+    h = 1e-3
+    tl_y, tl_k, ad_y, ad_k = _jacobians(lib, mech, y, kc, h)
+    mp.mp.dps = 60
+    ym = mp.matrix([mp.mpf(v) for v in y])
+    km = [mp.mpf(v) for v in kc]
+    for j in range(dm.nv + dm.nr):
+        if j < dm.nv:
+            d = mp.mpf(10) ** -25 * max(abs(ym[j]), mp.mpf(1))
+            yp, yn = ym.copy(), ym.copy()
+            yp[j] += d
+            yn[j] -= d
+            col = (_step_mp(dm, yp, km, h) - _step_mp(dm, yn, km, h)) / (2 * d)
+            tl, ad = tl_y[:, j], ad_y[:, j]
+        else:
+            r = j - dm.nv
+            d = mp.mpf(10) ** -25 * max(abs(km[r]), mp.mpf(1e-300))
+            kp, kn = list(km), list(km)
+            kp[r] += d
+            kn[r] -= d
+            col = (_step_mp(dm, ym, kp, h) - _step_mp(dm, ym, kn, h)) / (2 * d)
+            tl, ad = tl_k[:, r], ad_k[:, r]
+        col = np.array([float(c) for c in col])
+        sc = max(np.abs(col).max(), 1e-300)
+        assert np.abs(tl - col).max() <= 1e-7 * sc, (j, "tangent")
+        assert np.abs(ad - col).max() <= 1e-7 * sc, (j, "adjoint")
 
 
 @pytest.mark.parametrize("mech", MECHS)

@@ -9,6 +9,9 @@ Tolerances:
 * free-running: |gpu - oracle| <= rtol |oracle| + atol per species for every
   cell whose step sequence matches, and the cells whose sequence diverges
   stay within 10 (rtol |oracle| + atol).
+The *_rodas3 libraries are Chapman and small_strato with the 4-stage RODAS-3
+tableau (src/mkpp/rosenbrock.py:71-82); the oracle runs the same tableau
+from their plans.
 """
 import numpy as np
 import pytest
@@ -18,7 +21,7 @@ from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-SIZES = {"chapman": 512, "small_strato": 512, "saprc99": 48}
+SIZES = {"chapman": 512, "small_strato": 512, "saprc99": 48, "chapman_rodas3": 512, "small_strato_rodas3": 512}
 
 
 def _torch():

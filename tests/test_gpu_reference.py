@@ -6,7 +6,9 @@ integrate() (tests/test_oracle_reference.py).  Here the two ends meet
 directly: the reference's SolverKernels<D>::integrate(), regenerated by its
 compiler and built on the host cores (oracle/ref_build.py, the same build
 bench.py times as the CPU baseline), against the GPU's free-running
-integrate on the same seeded cells.  Skipped where that build is absent.
+integrate on the same seeded cells, with the ROS-3 tableau and, for Chapman
+and small_strato, RODAS-3 (the reference compiler's --solver rodas3 against
+the *_rodas3 libraries).  Skipped where that build is absent.
 
 Free-running, an accept/reject decision can flip on round-off, after which a
 cell follows another step sequence within the tolerances, so the bounds are
@@ -23,7 +25,7 @@ from mkpp_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
 
-CELLS = {"chapman": 512, "small_strato": 512, "saprc99": 48}
+CELLS = {"chapman": 512, "small_strato": 512, "saprc99": 48, "chapman_rodas3": 512, "small_strato_rodas3": 512}
 
 
 def _run(mech):
@@ -33,7 +35,7 @@ def _run(mech):
     from mkpp_gb300.emitter.plan import load_raw
     from oracle import ref_build
 
-    ref = ref_build.load(mech)
+    ref = ref_build.load(mech) if mech in ref_build.MECHS else ref_build.ensure(mech)
     if ref is None:
         pytest.skip("the reference's generated solver is not built on this machine")
     w = workloads.make(mech, CELLS[mech])
@@ -49,7 +51,7 @@ def _run(mech):
     return got, ref_conc, ok, np.array(raw["rtol"])[:, None], np.array(raw["atol"])[:, None]
 
 
-@pytest.mark.parametrize("mech", ["chapman", "small_strato"])
+@pytest.mark.parametrize("mech", ["chapman", "small_strato", "chapman_rodas3", "small_strato_rodas3"])
 def test_free_running_matches_reference_solver(built_libs, mech):
     got, ref, ok, rtol, atol = _run(mech)
     assert ok.mean() > 0.9

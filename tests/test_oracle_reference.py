@@ -8,7 +8,10 @@ These tests compare the oracle port with that build on seeded inputs:
   src/mkpp/templates/kernels.j2) to round-off, which pins the rate constants,
   the flux products and the Jacobian pattern of every reaction;
 * ``SolverKernels<D>::integrate()`` (src/mkpp/templates/integrate.j2) over one
-  host step.  Chapman and the stratospheric mechanism agree to round-off.
+  host step.  Chapman and the stratospheric mechanism agree to round-off,
+  with the default ROS-3 tableau and with RODAS-3 (the reference compiler's
+  ``--solver rodas3``, src/mkpp/rosenbrock.py:71-82, against the
+  *_rodas3 plans).
   SAPRC99 as shipped has rate constants up to 1e37 (reactions 11, 32, 69),
   where a one-ulp difference in k moves the solution by 1e-6 and can change
   the accepted step sequence.  There the bound is statistical, the same two
@@ -65,7 +68,12 @@ def test_tendencies_and_jacobian_match_reference(mech):
         assert not np.any(J1[~nz])
 
 
-@pytest.mark.parametrize("mech", ["chapman", "small_strato"])
+# RODAS-3's stage coefficients (C/h up to 4/h) amplify round-off more than
+# ROS-3's: small_strato_rodas3 measured 1.9e-10 at worst (median 1e-15).
+INTEGRATE_BOUND = {"chapman": 1e-12, "small_strato": 1e-12, "chapman_rodas3": 1e-12, "small_strato_rodas3": 1e-9}
+
+
+@pytest.mark.parametrize("mech", list(INTEGRATE_BOUND))
 def test_integrate_matches_reference(mech):
     ref = _ref(mech)
     o = Oracle(mech)
@@ -76,7 +84,7 @@ def test_integrate_matches_reference(mech):
     rr = ref.integrate(b, w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
     assert np.all(ro["status"] == 0)
     rel = np.abs(ro["conc"] - rr["conc"]) / np.maximum(np.abs(rr["conc"]), 1.0)
-    assert rel.max() < 1e-12
+    assert rel.max() < INTEGRATE_BOUND[mech]
 
 
 # Bounds per mechanism, from seeded 64-cell samples (measured: element median

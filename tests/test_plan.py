@@ -59,7 +59,7 @@ def test_reduced_plan_invariants(mech):
     assert written == set(range(len(p.lu_slots)))
 
 
-@pytest.mark.parametrize("mech", MECHS + ["chapman_shipped"])
+@pytest.mark.parametrize("mech", MECHS + ["chapman_shipped", "chapman_rodas3", "small_strato_rodas3"])
 def test_generated_header_is_current(mech):
     plan = load(mech)
     text = cuda_emitter.emit_mechanism(plan)
