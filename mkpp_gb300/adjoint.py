@@ -131,6 +131,82 @@ class RosenbrockSolve(torch.autograd.Function):
         return out
 
 
+class WindowGradient:
+    """Gradient of a loss on the state after several host steps (one
+    integrate() call per host step, each with its own rate constants), with
+    two levels of checkpoints so that memory stays bounded at any cell count:
+
+    * level 1, in the forward: the state at every host-step boundary
+      ((host_steps + 1) x species x cells doubles), the integration itself
+      one persistent launch per host step;
+    * level 2, in the backward, host steps last to first and cells in chunks
+      of ``chunk``: the accepted steps of the chunk's host step are recomputed
+      from its level-1 state (mkpp_gpu_integrate_checkpoint, the same
+      controller and arithmetic, so the same steps and states as the forward)
+      and swept in reverse (mkpp_gpu_adjoint), which turns lambda at the end
+      of the host step into lambda at its start and gives dL/dk of that host
+      step.
+
+    Checkpoint memory is chunk x cap x variable species doubles, whatever the
+    cell count.  A cell whose host step needs more than ``cap`` accepted steps
+    ends with status 5 in ``status`` and non-finite gradients."""
+
+    def __init__(self, mechanism: str, ncells: int, host_steps: int, device, cap: int = 768,
+                 chunk: int = 65536):
+        self.mechanism = mechanism
+        self.lib = load_library(mechanism)
+        self.sizes = sizes(mechanism)
+        self.n = ncells
+        self.hs = host_steps
+        self.cap = cap
+        self.chunk = min(chunk, ncells)
+        self.device = device
+        self.bounds = torch.empty((host_steps + 1, self.sizes.species, ncells), dtype=torch.float64, device=device)
+        self.fixed = _fixed_rows(mechanism, device)
+        self.status = torch.zeros(ncells, dtype=torch.int32, device=device)
+
+    def forward(self, conc, ktab, dt, seed, max_attempts=20000, solver=None):
+        """Integrates conc in place over the host steps (ktab [host step]
+        [reaction][cell]), keeping every boundary state."""
+        from .api import DeviceSolver
+
+        s = solver or DeviceSolver(self.mechanism)
+        self.dt, self.seed, self.max_attempts = dt, seed, max_attempts
+        self.bounds[0].copy_(conc)
+        st = torch.zeros(self.n, dtype=torch.int32, device=conc.device)
+        for h in range(self.hs):
+            s.integrate_k(conc, ktab[h], dt, seed=seed, max_attempts=max_attempts, status=st)
+            self.bounds[h + 1].copy_(conc)
+        self.forward_status = st
+        return conc
+
+    def backward(self, ktab, lam_end):
+        """(dL/dconc0 [species][cell], dL/dk [host step][reaction][cell])
+        from lam_end = dL/dconc_end.  Fixed species pass their lambda through
+        (integrate() leaves them unchanged; they act through ktab)."""
+        n, c = self.n, self.chunk
+        lam = lam_end.detach().clone().contiguous()
+        gk = torch.empty((self.hs, self.sizes.reactions, n), dtype=torch.float64, device=lam.device)
+        ck = Checkpoints(self.mechanism, c, self.cap, lam.device)
+        self.status.zero_()
+        for h in reversed(range(self.hs)):
+            for c0 in range(0, n, c):
+                c1 = min(c0 + c, n)
+                if c1 - c0 != ck.n:
+                    ck = Checkpoints(self.mechanism, c1 - c0, self.cap, lam.device)
+                y = self.bounds[h][:, c0:c1].contiguous()
+                k = ktab[h][:, c0:c1].contiguous()
+                ck.forward(y, k, self.dt, self.seed, self.max_attempts)
+                lam_c = lam[:, c0:c1].contiguous()
+                gc, gkc = ck.adjoint(k, lam_c)
+                gc[self.fixed] = lam_c[self.fixed]
+                lam[:, c0:c1] = gc
+                gk[h][:, c0:c1] = gkc
+                bad = ck.status != 0
+                self.status[c0:c1] = torch.where((self.status[c0:c1] == 0) & bad, ck.status, self.status[c0:c1])
+        return lam, gk
+
+
 def _fixed_rows(mechanism: str, device):
     """Indices of the fixed species in the (species, cells) layout."""
     fixed = load_raw(mechanism)["fixed"]
