@@ -106,6 +106,16 @@ int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* r
  * depend on it (cells are independent); it reads back num_cells x 2 ints per
  * call.  enable 0 turns it off and forgets the counts. */
 int mkpp_set_cost_order(mkpp_handle_t handle, int enable);
+/* Step-size carry-over (default off; no reference entry: the reference
+ * restarts every integrate() at dt * initial_step_seed and lists carried
+ * step estimates as future work, SCALING_OPTIMIZATION_REPORT.md:27-29).
+ * When on, each mkpp_integrate starts every cell at the step size its
+ * previous call on this handle ended with (the controller's proposal after
+ * the last accepted step, or the step wanted before a last step cut short to
+ * end at dt), the first call after enabling at dt * seed.  It changes the
+ * step sequence, so results differ from the reference's within the
+ * tolerances; it removes the ramp from dt * seed at every call. */
+int mkpp_set_dt_carryover(mkpp_handle_t handle, int enable);
 
 /* ---- Mechanism metadata (no reference C entry; compile-time constants of
  * the generated SolverKernels, header.j2:127-186) ------------------------ */
@@ -175,6 +185,17 @@ int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab,
                          const int* cell_order, int* status, int* accepted, int* rejected,
                          void* workspace, size_t workspace_bytes, void* stream);
 
+/* mkpp_gpu_integrate_k with step-size carry-over (see mkpp_set_dt_carryover):
+ * dt_carry [num_cells] doubles on the device, in/out.  dt_carry[c] > 0 starts
+ * cell c's first call at that step size (0: at dt * seed), later calls of the
+ * launch start from the previous call's carry, and the last one is written
+ * back.  No reference counterpart. */
+int mkpp_gpu_integrate_carry(size_t num_cells, double* conc, const double* ktab,
+                             size_t k_step_stride, int steps, double dt, double seed,
+                             int max_attempts, int mode, const int* cell_order, int* status,
+                             int* accepted, int* rejected, double* dt_carry, void* workspace,
+                             size_t workspace_bytes, void* stream);
+
 /* Same as mkpp_gpu_integrate_k, also recording every attempt's step size and
  * accept flag (log_h/log_acc[attempt * num_cells + cell], log_n[cell]) for
  * step-sequence replay; plain mode only. */
@@ -239,22 +260,27 @@ int mkpp_gpu_tangent(size_t num_cells, const double* ktab, int ckpt_cap, const d
                      const double* delta_k, double* delta_conc, void* workspace,
                      size_t workspace_bytes, void* stream);
 
-/* Allocation-free integrate (no counterpart in the reference).  For callers
- * that cannot allocate device memory at the point where they integrate: a
- * host model that records its time step into a CUDA graph (cudaMalloc is not
- * allowed while a stream is being captured), or one whose memory pool owns
- * all free device memory.  Same semantics as mkpp_gpu_integrate_k in plain
- * mode (one thread per cell), but the LU and stage scratch is a static
- * device array inside the library, sized for MKPP_NOALLOC_MAX_CELLS cells
- * (for SAPRC99 1024 x 2226 doubles, 18 MB), which every GPU that loads the
- * library holds until the process exits.  Larger num_cells is rejected with
- * MKPP_ERROR_INVALID_ARGUMENT and a message on stderr.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU (other streams,
- * other host threads) race and must not be issued.  Nothing in the array
- * needs clearing between calls; each cell's slots are written before they
- * are read.  Makes no cudaMalloc or cudaFree call. */
+/* Allocation-free integrate (no counterpart in the reference).  For host
+ * models that must not allocate device memory at the point where they call
+ * the chemistry: one that hands all free device memory to its own pool
+ * allocator at start-up, or one whose time loop must not call cudaMalloc or
+ * cudaFree because those calls synchronise the whole device and stall the
+ * model's other streams.  Same semantics as mkpp_gpu_integrate_k in plain
+ * mode (one thread per cell); the caller passes the inputs and outputs, and
+ * the LU and stage scratch is a static device array inside the library,
+ * sized for MKPP_NOALLOC_MAX_CELLS cells: 1024 x NSLOTS doubles (SAPRC99
+ * 18.2 MB, saprcnov 17.3 MB, TS1 85.2 MB, saprc99_mini 1.2 MB; Chapman and
+ * small_strato keep their store in registers and use none), which every GPU
+ * that loads the library holds until the process exits.  Larger num_cells
+ * is rejected with MKPP_ERROR_INVALID_ARGUMENT and a message on stderr.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and keeps it for the
+ * process; make that first call before any stream capture, and make no call
+ * after a cudaDeviceReset of that device, which leaves the kept address
+ * stale.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must not be issued.  Nothing in the
+ * array needs clearing between calls; each cell's slots are written before
+ * they are read.  Makes no cudaMalloc or cudaFree call. */
 #define MKPP_NOALLOC_MAX_CELLS 1024
 int mkpp_gpu_integrate_noalloc(size_t num_cells, double* conc, const double* ktab,
                                size_t k_step_stride, int steps, double dt, double seed,

@@ -88,6 +88,9 @@ SIGNATURES = [
     ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_set_cost_order", _i, [_vp, _i]),
+    ("mkpp_set_dt_carryover", _i, [_vp, _i]),
+    ("mkpp_gpu_integrate_carry", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
+                                      _vp]),
     ("mkpp_mechanism_flags", _i, [_vp, _vp]),
     ("mkpp_mechanism_tolerances", _i, [_vp, _vp]),
     ("mkpp_set_tail_parking", _i, [_i]),
@@ -237,6 +240,11 @@ class MechanismContext:
         """Hand out the previous call's most expensive cells first."""
         self._check(self.lib.mkpp_set_cost_order(self.handle, C.c_int(1 if enable else 0)))
 
+    def set_dt_carryover(self, enable: bool = True):
+        """Start each call at the step size the previous call ended with
+        (changes results within the tolerances; off by default)."""
+        self._check(self.lib.mkpp_set_dt_carryover(self.handle, C.c_int(1 if enable else 0)))
+
     # --- compute ---------------------------------------------------------
     def integrate(self, dt: float):
         self._check(self.lib.mkpp_integrate(self.handle, C.c_double(dt)))
@@ -336,16 +344,24 @@ class DeviceSolver:
         return ktab, status
 
     def integrate_k(self, conc, ktab, dt, steps=1, seed=None, max_attempts=20000, mode="persistent",
-                    status=None, accepted=None, rejected=None, order=None, k_step_stride=0):
+                    status=None, accepted=None, rejected=None, order=None, k_step_stride=0, dt_carry=None):
+        """dt_carry: optional float64 [cells] device tensor, in/out, for
+        step-size carry-over across calls (mkpp_gpu_integrate_carry)."""
         torch = self.torch
         ns, n = conc.shape
         if seed is None:
             seed = self.default_seed
         ws = self.workspace(n)
-        rc = self.lib.mkpp_gpu_integrate_k(
-            C.c_size_t(n), _ptr(conc), _ptr(ktab), C.c_size_t(k_step_stride), C.c_int(steps), C.c_double(dt),
-            C.c_double(seed), C.c_int(max_attempts), C.c_int(MODES[mode]), _ptr(order), _ptr(status), _ptr(accepted), _ptr(rejected),
-            _ptr(ws), C.c_size_t(ws.numel()), self._stream())
+        common = (C.c_size_t(n), _ptr(conc), _ptr(ktab), C.c_size_t(k_step_stride), C.c_int(steps), C.c_double(dt),
+                  C.c_double(seed), C.c_int(max_attempts), C.c_int(MODES[mode]), _ptr(order), _ptr(status),
+                  _ptr(accepted), _ptr(rejected))
+        if dt_carry is None:
+            rc = self.lib.mkpp_gpu_integrate_k(*common, _ptr(ws), C.c_size_t(ws.numel()), self._stream())
+        else:
+            if dt_carry.dtype != torch.float64 or dt_carry.shape != (n,) or not dt_carry.is_contiguous():
+                raise ValueError("dt_carry must be a contiguous float64 tensor of one value per cell")
+            rc = self.lib.mkpp_gpu_integrate_carry(*common, _ptr(dt_carry), _ptr(ws), C.c_size_t(ws.numel()),
+                                                  self._stream())
         self._check(rc)
 
     def integrate(self, conc, dt, steps=1, temp=None, rho=None, rh=None, clw=None, param=None, seed=None,

@@ -42,6 +42,7 @@ struct DeviceBuffers {
   int* accepted = nullptr;
   int* rejected = nullptr;
   int* order = nullptr;        // queue position -> cell (cost ordering)
+  double* dt_carry = nullptr;  // carried step size per cell (mkpp_set_dt_carryover)
   void* workspace = nullptr;
   size_t workspace_bytes = 0;  // grows when a launch-tuning change enlarges the grid
 };
@@ -66,6 +67,10 @@ struct mkpp_handle_s {
   // Cost ordering (mkpp_set_cost_order): the persistent queue hands out the
   // cells that needed the most attempts in the previous call first.
   bool cost_order = false;
+  // Step-size carry-over (mkpp_set_dt_carryover): each call starts every
+  // cell at the step size its previous call ended with.
+  bool dt_carryover = false;
+  bool dt_carry_reset = false;  // zero the carried step sizes before the next call
   std::vector<int> cost;       // attempts per cell of the previous call
   std::vector<int> rejected;   // staging for the read-back
   std::vector<int> order;      // queue position -> cell
@@ -261,6 +266,9 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
 // obtained once per device with cudaGetSymbolAddress.
 // ---------------------------------------------------------------------------
 constexpr int kNoAllocMaxCells = MKPP_NOALLOC_MAX_CELLS;
+// The plain launch gives every block kBlock cells of scratch, so the array
+// covers the last block only when the capacity is a whole number of blocks.
+static_assert(kNoAllocMaxCells % mkpp::kBlock == 0, "noalloc capacity must be a multiple of the block size");
 constexpr size_t kNoAllocDoubles = StoreInfo::kTile ? (size_t)kNoAllocMaxCells * Mech::NSLOTS : 1;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
@@ -332,7 +340,7 @@ int mkpp_create_handle(mkpp_handle_t* handle_out, size_t num_cells) {
 static void free_device(DeviceBuffers& d) {
   for (void* p : {(void*)d.conc, (void*)d.temp, (void*)d.rho, (void*)d.rh, (void*)d.clw, (void*)d.param,
                   (void*)d.ktab, (void*)d.out, (void*)d.status, (void*)d.accepted, (void*)d.rejected,
-                  (void*)d.order, d.workspace})
+                  (void*)d.order, (void*)d.dt_carry, d.workspace})
     if (p) cudaFree(p);
   d = DeviceBuffers();
 }
@@ -547,6 +555,15 @@ int mkpp_integrate(mkpp_handle_t handle, double dt) {
     MKPP_CUDA(h, cudaMemcpyAsync(d.order, h->order.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     args.order = d.order;
   }
+  if (h->dt_carryover) {
+    if (!d.dt_carry) {
+      MKPP_CUDA(h, cudaMalloc(&d.dt_carry, n * sizeof(double)));
+      h->dt_carry_reset = true;
+    }
+    if (h->dt_carry_reset) MKPP_CUDA(h, cudaMemsetAsync(d.dt_carry, 0, n * sizeof(double), h->stream));
+    h->dt_carry_reset = false;
+    args.dt_carry = d.dt_carry;
+  }
   rc = launch_integrate(args, h->mode, d.workspace, h->stream);
   if (rc != MKPP_SUCCESS) return device_fail(h, cudaGetLastError(), "integrate kernel launch");
   MKPP_CUDA(h, cudaMemcpyAsync(h->conc, d.conc, n * Mech::NS * sizeof(double), cudaMemcpyDeviceToHost,
@@ -568,6 +585,13 @@ int mkpp_set_cost_order(mkpp_handle_t handle, int enable) {
   if (!handle) return MKPP_ERROR_NULL_POINTER;
   handle->cost_order = enable != 0;
   handle->cost.clear();
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_dt_carryover(mkpp_handle_t handle, int enable) {
+  if (!handle) return MKPP_ERROR_NULL_POINTER;
+  handle->dt_carryover = enable != 0;
+  handle->dt_carry_reset = true;
   return MKPP_SUCCESS;
 }
 
@@ -818,6 +842,23 @@ int mkpp_gpu_integrate_k(size_t num_cells, double* conc, const double* ktab, siz
   mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
   a.order = cell_order;
   a.k_step_stride = k_step_stride;
+  return launch_integrate(a, mode, workspace, (cudaStream_t)stream);
+}
+
+int mkpp_gpu_integrate_carry(size_t num_cells, double* conc, const double* ktab, size_t k_step_stride, int steps,
+                             double dt, double seed, int max_attempts, int mode, const int* cell_order,
+                             int* status, int* accepted, int* rejected, double* dt_carry, void* workspace,
+                             size_t workspace_bytes_, void* stream) {
+  if (!dt_carry) return MKPP_ERROR_NULL_POINTER;
+  const int rc = check_integrate_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, workspace, workspace_bytes_);
+  if (rc != MKPP_SUCCESS) return rc;
+  const NvtxRange range(kDispatchRange);
+  if (mode != 0 && mode != 1) return MKPP_ERROR_INVALID_ARGUMENT;
+  if (k_step_stride != 0 && k_step_stride < num_cells * Mech::NR) return MKPP_ERROR_INVALID_ARGUMENT;
+  mkpp::LaunchArgs a = make_args(num_cells, conc, ktab, steps, dt, seed, max_attempts, status, accepted, rejected);
+  a.order = cell_order;
+  a.k_step_stride = k_step_stride;
+  a.dt_carry = dt_carry;
   return launch_integrate(a, mode, workspace, (cudaStream_t)stream);
 }
 

@@ -55,12 +55,18 @@ struct LaunchArgs {
   unsigned int* active;
   int tail_after;
   unsigned int tail_cells;
+  // Step-size carry-over across integrate() calls (null: off, the
+  // reference's controller): dt_carry[c] > 0 starts the cell's first call
+  // at that step size instead of dt * seed, each later call of the launch
+  // starts from the previous call's carry, and the last call's carry is
+  // written back (Controller::carry_out).
+  double* dt_carry;
 };
 
 // Controller state of a parked cell (see LaunchArgs::defer).
 struct Deferred {
-  int cell, step, attempts, nacc, nrej, flags;  // flags: 1 reject_last, 2 reject_more, 4 zero pivot
-  double t, dt;
+  int cell, step, attempts, nacc, nrej, flags;  // flags: 1 reject_last, 2 reject_more, 4 zero pivot, 8 cut
+  double t, dt, want;
 };
 
 struct RateArgs {
@@ -155,23 +161,34 @@ __device__ __forceinline__ RegStore<N> make_store(double*, RegStore<N>*) {
 // ---------------------------------------------------------------------------
 struct Controller {
   double t, dt, dt_total, h_min;
+  double want;       // the step size chosen before the end-of-call cut
   bool reject_last, reject_more;
+  bool cut;          // the last attempt was cut short to end at dt_total
   int attempts;
 
-  __device__ __forceinline__ void start(double total, double seed) {
+  // carry > 0 and finite: start at fmin(carry, total) (step-size carry-over,
+  // off by default); otherwise at total * seed as integrate.j2:80 does.
+  __device__ __forceinline__ void start(double total, double seed, double carry = 0.0) {
     dt_total = total;
     h_min = total * 1.0e-15;
     t = 0.0;
-    dt = total * seed;
-    reject_last = reject_more = false;
+    dt = (carry > 0.0 && finite(carry)) ? fmin(carry, total) : total * seed;
+    want = dt;
+    reject_last = reject_more = cut = false;
     attempts = 0;
   }
   __device__ __forceinline__ bool running() const { return t < dt_total; }
   // Step size of the next attempt (integrate.j2:85: dt = min(dt, dt_total - t)).
   __device__ __forceinline__ double next_h() {
+    want = dt;
+    cut = dt_total - t < dt;
     dt = fmin(dt, dt_total - t);
     return dt;
   }
+  // Step size carried into the next call once this one has ended: the
+  // proposal after its last accepted step, or, when that step was cut short
+  // to end at dt_total, the step size wanted before the cut.
+  __device__ __forceinline__ double carry_out() const { return cut ? want : dt; }
   // Accept/reject bookkeeping (integrate.j2:335-379); returns true on accept.
   template <class Mech>
   __device__ __forceinline__ bool update(double err) {
@@ -248,11 +265,12 @@ __device__ __forceinline__ int integrate_cell(SA& S, const LaunchArgs& a, size_t
   int logged = 0;
   bool capped = false, zero_pivot = false;
   nacc = nrej = 0;
+  double carry = a.dt_carry ? a.dt_carry[c] : 0.0;
   for (int step = 0; step < a.steps && !capped; ++step) {
     load_rates<Mech>(a, c, step, S);
     auto k = [&](int r) { return S[Mech::KT + r]; };
     Controller ctl;
-    ctl.start(a.dt, a.seed);
+    ctl.start(a.dt, a.seed, carry);
     while (ctl.running()) {
       if (ctl.attempts >= a.max_attempts) {
         capped = true;
@@ -275,7 +293,9 @@ __device__ __forceinline__ int integrate_cell(SA& S, const LaunchArgs& a, size_t
         ++nrej;
       }
     }
+    if (a.dt_carry) carry = ctl.carry_out();
   }
+  if (a.dt_carry) a.dt_carry[c] = carry;
   if (a.log_n) a.log_n[c] = logged;
   return final_status<Mech>(S, capped, zero_pivot);
 }
@@ -351,7 +371,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
             load_state<Mech>(a.conc, (size_t)cell, n, S);
             load_rates<Mech>(a, (size_t)cell, 0, S);
           }
-          ctl.start(a.dt, a.seed);
+          ctl.start(a.dt, a.seed, a.dt_carry && !flagged ? a.dt_carry[cell] : 0.0);
         }
       }
       if constexpr (TAIL) {
@@ -381,7 +401,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
         }
         if (!ctl.running()) {
           if (++step < a.steps) {
-            ctl.start(a.dt, a.seed);
+            ctl.start(a.dt, a.seed, a.dt_carry ? ctl.carry_out() : 0.0);
             load_rates<Mech>(a, (size_t)cell, step, S);
           } else {
             done = true;
@@ -398,9 +418,10 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
           d.attempts = ctl.attempts;
           d.nacc = nacc;
           d.nrej = nrej;
-          d.flags = (ctl.reject_last ? 1 : 0) | (ctl.reject_more ? 2 : 0) | (zero_pivot ? 4 : 0);
+          d.flags = (ctl.reject_last ? 1 : 0) | (ctl.reject_more ? 2 : 0) | (zero_pivot ? 4 : 0) | (ctl.cut ? 8 : 0);
           d.t = ctl.t;
           d.dt = ctl.dt;
+          d.want = ctl.want;
           a.defer[slot] = d;
           store_state<Mech>(a.conc, (size_t)cell, n, S);
           cell = -1;
@@ -413,6 +434,7 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
       const size_t cc = (size_t)cell;
       if (!flagged) {
         store_state<Mech>(a.conc, cc, n, S);
+        if (a.dt_carry) a.dt_carry[cc] = ctl.carry_out();
         if (a.status) a.status[cc] = final_status<Mech>(S, capped, zero_pivot);
         if (a.n_accept) a.n_accept[cc] = nacc;
         if (a.n_reject) a.n_reject[cc] = nrej;
@@ -450,9 +472,11 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
     ctl.start(a.dt, a.seed);
     ctl.t = d.t;
     ctl.dt = d.dt;
+    ctl.want = d.want;
     ctl.attempts = d.attempts;
     ctl.reject_last = d.flags & 1;
     ctl.reject_more = (d.flags & 2) != 0;
+    ctl.cut = (d.flags & 8) != 0;
     bool zero_pivot = (d.flags & 4) != 0, capped = false;
     int nacc = d.nacc, nrej = d.nrej;
     for (int step = d.step; step < a.steps;) {
@@ -477,13 +501,14 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
         }
       }
       if (capped || ++step >= a.steps) break;
-      ctl.start(a.dt, a.seed);
+      ctl.start(a.dt, a.seed, a.dt_carry ? ctl.carry_out() : 0.0);
     }
     bool fin = true;
     for (int i = lane; i < Mech::NV; i += 32) fin = fin && finite(S[Mech::Y + i]);
     fin = __all_sync(0xffffffffu, fin);
     for (int i = lane; i < Mech::NV; i += 32) a.conc[c + n * Mech::var_phys(i)] = S[Mech::Y + i];
     if (lane == 0) {
+      if (a.dt_carry) a.dt_carry[c] = ctl.carry_out();
       const int status = !fin ? CELL_ERR_NUMERICAL_FAILURE
                               : (capped ? CELL_ERR_CONVERGENCE_FAILURE
                                         : (zero_pivot ? CELL_ERR_SINGULAR_MATRIX : CELL_SUCCESS));

@@ -267,13 +267,23 @@ static void free_scratch(oracle_scratch* s) {
  * every attempt at [a * ncells + c] up to log_cap.  With replay_n != NULL the
  * step sequence is not chosen by the controller but read from replay_h /
  * replay_acc (same layout), replay_n[c] attempts for cell c.
+ * dt_carry (optional, [ncells] in/out): step-size carry-over across
+ * integrate() calls, a non-parity option of this build (the reference
+ * restarts every call at dt_total * seed and lists carried step estimates as
+ * future work, SCALING_OPTIMIZATION_REPORT.md:27-29).  A call starts at
+ * fmin(carry, dt_total) where carry > 0 and finite, else at dt_total * seed.
+ * What carries into the next call (and, after the last one, is written
+ * back) is the controller's proposal after the call's last accepted step,
+ * or, if that step was cut short to end at dt_total, the step size the
+ * controller wanted before the cut.
  * Returns the number of cells with a non-zero status.
  */
 int mkpp_oracle_integrate(const oracle_plan* p, int ncells, double* conc, const double* ktab,
                           const double* dktab, int ndk, double dt_total, int steps, double seed,
                           int max_attempts, int nthreads, int* status, int* accepted, int* rejected,
                           double* log_h, unsigned char* log_acc, int* log_n, int log_cap,
-                          const double* replay_h, const unsigned char* replay_acc, const int* replay_n) {
+                          const double* replay_h, const unsigned char* replay_acc, const int* replay_n,
+                          double* dt_carry) {
   int failures = 0;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -304,14 +314,18 @@ int mkpp_oracle_integrate(const oracle_plan* p, int ncells, double* conc, const 
           if (replay_acc[(size_t)a * ncells + c]) { accept_step(p, &s, state); ++nacc; } else { ++nrej; }
         }
       } else {
+        double carry = dt_carry ? dt_carry[c] : 0.0;
         for (int step = 0; step < steps && !st; ++step) {
           /* integrate.j2:71-84 */
           const double h_min = dt_total * 1.0e-15;
           double t = 0.0;
-          double dtc = dt_total * seed;
+          double dtc = (carry > 0.0 && isfinite(carry)) ? fmin(carry, dt_total) : dt_total * seed;
           int reject_last = 0, reject_more = 0, attempts = 0;
+          double dtc_last = 0.0, want_last = 0.0;
+          double want = dtc; /* the controller's step before the end-of-call cut */
           while (t < dt_total) {
             if (attempts >= max_attempts) { st = 3; break; }
+            want = dtc;
             dtc = fmin(dtc, dt_total - t);
             const double err = attempt(p, &s, state, k, dk, dtc);
             const double factor = growth(p, err);
@@ -324,6 +338,8 @@ int mkpp_oracle_integrate(const oracle_plan* p, int ncells, double* conc, const 
             }
             if (acc) {
               accept_step(p, &s, state);
+              dtc_last = dtc;
+              want_last = want;
               t += dtc;
               double next_dt = fmax(h_min, fmin(dtc * factor, dt_total));
               if (reject_last) next_dt = fmin(next_dt, dtc);
@@ -338,7 +354,11 @@ int mkpp_oracle_integrate(const oracle_plan* p, int ncells, double* conc, const 
               ++nrej;
             }
           }
+          /* a last step cut to reach dt_total says nothing about the step
+             size: carry the controller's step before the cut instead */
+          if (dt_carry) carry = (dtc_last < want_last) ? want_last : dtc;
         }
+        if (dt_carry) dt_carry[c] = carry;
       }
       for (int i = 0; i < p->ns; ++i) conc[(size_t)i * ncells + c] = state[i];
       if (!st) for (int i = 0; i < p->ns; ++i) if (!isfinite(state[i])) st = 4;

@@ -210,8 +210,11 @@ class Oracle:
         return k, dk
 
     def integrate(self, conc, dt, steps=1, temp=None, rho=None, rh=None, clw=None, param=None,
-                  seed=None, max_attempts=20000, nthreads=0, log_cap=0, replay=None, k=None, dk=None):
-        """Integrate in place a (species x cells) array; returns a dict of diagnostics."""
+                  seed=None, max_attempts=20000, nthreads=0, log_cap=0, replay=None, k=None, dk=None,
+                  dt_carry=None):
+        """Integrate in place a (species x cells) array; returns a dict of diagnostics.
+        dt_carry: optional float64 [cells] array, in/out, for step-size
+        carry-over across integrate() calls (0: start at dt * seed)."""
         conc = np.ascontiguousarray(conc, dtype=np.float64)
         ns, n = conc.shape
         assert ns == self.ns
@@ -229,6 +232,8 @@ class Oracle:
             la = np.zeros((log_cap, n), np.uint8)
             ln = np.zeros(n, np.int32)
             out.update(log_h=lh, log_acc=la, log_n=ln)
+        if dt_carry is not None:
+            assert dt_carry.dtype == np.float64 and dt_carry.shape == (n,) and dt_carry.flags.c_contiguous
         rh_ = ra_ = rn_ = None
         if replay is not None:
             rh_ = np.ascontiguousarray(replay[0], dtype=np.float64)
@@ -243,7 +248,7 @@ class Oracle:
             C.byref(self.plan), C.c_int(n), p(conc), p(k), p(dk), C.c_int(self.ndk), C.c_double(dt),
             C.c_int(steps), C.c_double(self.seed if seed is None else seed), C.c_int(max_attempts),
             C.c_int(nthreads), p(status), p(acc), p(rej), p(lh), p(la), p(ln), C.c_int(log_cap),
-            p(rh_), p(ra_), p(rn_))
+            p(rh_), p(ra_), p(rn_), p(dt_carry))
         out["failures"] = fails
         out["conc"] = conc
         return out

@@ -26,7 +26,7 @@ def _cuda_available() -> bool:
 # allocation-free entry point last.  Other modules keep their place before them.
 GPU_ORDER = ("test_gpu_adjoint", "test_gpu_parity", "test_gpu_scale", "test_gpu_ts1", "test_gpu_tuning",
              "test_gpu_tangent", "test_gpu_mechanisms", "test_gpu_reference", "test_gpu_golden", "test_registry",
-             "test_solver_kernels", "test_gpu_window_adjoint", "test_zz_no_alloc")
+             "test_solver_kernels", "test_gpu_window_adjoint", "test_gpu_carry", "test_zz_no_alloc")
 
 
 def _gpu_rank(item):
