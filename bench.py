@@ -74,13 +74,21 @@ def parse():
     ap.add_argument("--cpu-cells", type=int, default=None,
                     help="cells in the bounded CPU sample (default max(4096, 64 x threads): every thread gets "
                          "at least one of the reference's 64-cell chunks per host step)")
+    ap.add_argument("--cpu-chunk", type=int, default=64,
+                    help="cells per static OpenMP chunk of the reference CPU solver (the reference's 64); a "
+                         "smaller chunk keeps every thread busy on a sample of fewer than 64 cells per thread")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--max-attempts", type=int, default=20000)
     ap.add_argument("--order", type=int, default=1, help="hand out cells most-expensive-first (previous window)")
     ap.add_argument("--forms-cells", type=int, default=65536, help="cells of the plain-vs-persistent comparison")
     ap.add_argument("--forms-host-steps", type=int, default=2, help="host steps of that comparison")
-    ap.add_argument("--adjoint-cells", type=int, default=65536, help="cells of the adjoint/forward measurement")
+    ap.add_argument("--adjoint-cells", type=int, default=None,
+                    help="cells of the adjoint/forward measurement (default: 65536 for one 3600 s integrate(); "
+                         "every cell for the window gradient)")
+    ap.add_argument("--adjoint-window", type=int, default=None,
+                    help="1: gradient of the whole window (every host step, two-level checkpoints, "
+                         "WindowGradient); 0: of one 3600 s integrate().  Default: the window for ts1")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--tangent", type=int, default=0,
                     help="also time the tangent sweep over the adjoint section's checkpoints (mkpp_gpu_tangent)")
@@ -230,6 +238,67 @@ def bulk_rate(mechanism: str, cells: int, attempts: int, stream=None, defer: int
             "attempts_per_s": att / (ms * 1e-3), "tflops": att * flops / (ms * 1e-3) / 1e12}
 
 
+def adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, window_ms) -> dict:
+    """Gradient of L = sum_c (O3_c(end) - O3t_c)^2 over the whole window (every
+    host step, each with its own rate constants) with respect to the initial
+    concentrations and the rate constants of every host step, through
+    WindowGradient: the forward keeps the host-step boundary states (one
+    persistent launch per host step); the backward recomputes each host step
+    of each chunk of cells with checkpoints at its accepted steps and sweeps
+    it in reverse.  Reported: backward / forward time, also against the
+    timed window's time for the same cells."""
+    import torch
+
+    from mkpp_gb300.adjoint import WindowGradient
+    from mkpp_gb300.api import DeviceSolver, sizes
+    from mkpp_gb300.emitter.plan import load_raw
+
+    raw = load_raw(w.mechanism)
+    n = w.ncells
+    na = min(n, args.adjoint_cells or n)
+    nv = sizes(w.mechanism).variable
+    cap = 1024
+    # Level-2 checkpoints of one chunk: at most 60 GB.
+    chunk = max(128, min(na, int(60e9 // (cap * (nv + 1) * 8)) // 128 * 128))
+    dev = conc0.device
+    k = ktab if na == n else ktab[:, :, :na].contiguous()
+    wg = WindowGradient(w.mechanism, na, hs, dev, cap=cap, chunk=chunk)
+    solver = DeviceSolver(w.mechanism)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with torch.cuda.stream(stream):
+        conc = conc0[:, :na].clone()
+        ev[0].record(stream)
+        wg.forward(conc, k, w.dt, seed, args.max_attempts, solver=solver)
+        ev[1].record(stream)
+        stream.synchronize()
+        o3 = raw["species"].index("O3")
+        rng = torch.Generator(device="cpu").manual_seed(2718)
+        target = conc[o3] * torch.exp(0.2 * torch.randn(na, generator=rng, dtype=torch.float64)).to(dev)
+        lam = torch.zeros_like(conc)
+        lam[o3] = 2.0 * (conc[o3] - target)
+        ev[2].record(stream)
+        gc, gk = wg.backward(k, lam)
+        ev[3].record(stream)
+        stream.synchronize()
+    fms, bms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+    st = wg.status.cpu().numpy()
+    fin = (torch.isfinite(gc).all(0) & torch.isfinite(gk).all(0).all(0)).double().mean().item()
+    out = {
+        "config": f"first {na} cells, {hs} host steps of {w.dt:g} s, loss sum (O3 - O3t)^2, O3t log-normal "
+                  f"sigma 0.2; two-level checkpoints (host-step boundaries; accepted steps of {chunk}-cell "
+                  f"chunks, cap {cap})",
+        "forward_ms": fms, "backward_ms": bms, "adjoint_over_forward": bms / fms,
+        "adjoint_over_window_forward": bms / (window_ms * na / n),
+        "cell_status_counts": np.bincount(st, minlength=6).tolist(),
+        "gradients": f"dL/dC0 for all species and dL/dk for all {len(raw['reactions'])} reactions of every "
+                     f"host step, FP64",
+        "finite_gradients_frac": fin,
+    }
+    del wg, gc, gk
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_sample_cells(args, threads: int) -> int:
     """Cells of the CPU sample: at least 4096, and at least one 64-cell chunk
     of the reference's static OpenMP schedule per thread."""
@@ -252,23 +321,25 @@ def cpu_runner(mechanism: str):
     return "port", Oracle(mechanism)
 
 
-def cpu_integrate(runner, sub, conc, first: int, last: int, threads: int) -> float:
+def cpu_integrate(runner, sub, conc, first: int, last: int, threads: int, chunk: int = 64) -> float:
     """Host steps [first, last) of every cell of `sub`, in place on conc;
     returns the seconds.  One OpenMP parallel region per host step, as the
     reference's host loop calls its dispatcher once per host step."""
+    extra = {"chunk": chunk} if chunk != 64 else {}
+    params = [sub.param_at(s) for s in range(first, last)]
     t0 = time.perf_counter()
-    for s in range(first, last):
-        runner.integrate(conc, sub.dt, temp=sub.temp, rho=sub.rho, rh=sub.rh, param=sub.param_at(s),
-                         nthreads=threads)
+    for par in params:
+        runner.integrate(conc, sub.dt, temp=sub.temp, rho=sub.rho, rh=sub.rh, param=par, nthreads=threads,
+                         **extra)
     return time.perf_counter() - t0
 
 
-def cpu_reference_sample(w, cells: int, host_steps: int, threads: int):
+def cpu_reference_sample(w, cells: int, host_steps: int, threads: int, chunk: int = 64):
     """Time the CPU implementation on the first `cells` cells of the workload,
     all host steps."""
     sub = w.subset(cells)
     kind, runner = cpu_runner(sub.mechanism)
-    el = cpu_integrate(runner, sub, sub.conc.copy(), 0, host_steps, threads)
+    el = cpu_integrate(runner, sub, sub.conc.copy(), 0, host_steps, threads, chunk)
     return kind, cells * host_steps / el, el
 
 
@@ -282,10 +353,10 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     cells = min(cpu_sample_cells(args, threads), w.ncells)
     kind, runner = cpu_runner(w.mechanism)
-    # Warm-up steps: one host step of one 64-cell chunk per thread.
-    warm = w.subset(min(64 * threads, w.ncells))
+    # Warm-up steps: one host step of one chunk per thread (at most the sample).
+    warm = w.subset(min(args.cpu_chunk * threads, cells))
     for _ in range(args.warmup):
-        cpu_integrate(runner, warm, warm.conc.copy(), 0, 1, threads)
+        cpu_integrate(runner, warm, warm.conc.copy(), 0, 1, threads, args.cpu_chunk)
     # Timed steps: together they integrate one whole window (all host steps)
     # of the sample, step i taking host steps [hs i / K, hs (i + 1) / K), so
     # the run stays bounded whatever K is while the sample keeps the cost mix
@@ -300,12 +371,12 @@ def run_reference(args, world, rank):
         for x in range(passes * i // args.steps, passes * (i + 1) // args.steps):
             if x % hs == 0:
                 conc = sub.conc.copy()
-            total += cpu_integrate(runner, sub, conc, x % hs, x % hs + 1, threads)
+            total += cpu_integrate(runner, sub, conc, x % hs, x % hs + 1, threads, args.cpu_chunk)
     value = cells * passes / total
     ms = total / args.steps * 1e3
     sample = (f"first {cells} of {w.ncells} cells x {hs} host steps of {w.dt:g} s"
               + (f" ({windows} windows)" if windows > 1 else "") + f", split over the {args.steps} timed steps; "
-              f"OpenMP static chunks of 64 cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+              f"OpenMP static chunks of {args.cpu_chunk} cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
               f"OMP_PLACES={os.environ.get('OMP_PLACES')}")
     line = {
         "impl": "reference", "metric": metric_for(w.mechanism), "value": value, "unit": UNIT, "n_gpus": world,
@@ -540,7 +611,12 @@ def main():
                                "persistent": dict(res["persistent"], form="persistent queue + cooperative hand-off, "
                                                                          "one launch for all host steps")}
 
-    if rank == 0 and not args.no_adjoint:
+    window_adjoint = args.adjoint_window if args.adjoint_window is not None else int(w.mechanism == "ts1")
+    if rank == 0 and not args.no_adjoint and window_adjoint:
+        with optional_section(result, "adjoint", True):
+            result["adjoint"] = adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, el_ms)
+            log(f"adjoint: {result['adjoint']}")
+    if rank == 0 and not args.no_adjoint and not window_adjoint:
         with optional_section(result, "adjoint", True):
             # Discrete adjoint (SAPRC99 adjoint configuration): first adjoint_cells
             # cells, one 3600 s integrate() with checkpoints at accepted steps, loss
@@ -552,7 +628,7 @@ def main():
             cap = 1536
             # Checkpoints hold cap x NV doubles per cell: at most 100 GB of them
             # (SAPRC99: 65536 cells = 63 GB; TS1 would need 168 GB for 65536).
-            na = min(n, args.adjoint_cells, int(100e9 // (cap * plan.n_var * 8)))
+            na = min(n, args.adjoint_cells or 65536, int(100e9 // (cap * plan.n_var * 8)))
             ca0 = conc0[:, :na].contiguous()
             ka = ktab[0, :, :na].contiguous()
             del ktab
@@ -651,15 +727,15 @@ def main():
         with optional_section(result, "cpu_baseline", True):
             threads = os.cpu_count() or 1
             cells = min(cpu_sample_cells(args, threads), n)
-            kind, v, el = cpu_reference_sample(w, cells, hs, threads)
+            kind, v, el = cpu_reference_sample(w, cells, hs, threads, args.cpu_chunk)
             log(f"cpu baseline ({kind}): {el:.1f} s")
             # The sample's cost mix against the whole run's, from the GPU's
             # attempt counters on the same cells (the CPU solver runs the
             # same controller, so it makes the same attempts up to round-off).
             result["cpu_baseline"] = {
                 "value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                "sample": f"first {cells} of {n} cells x {hs} host steps of {w.dt:g} s, OpenMP static chunks of 64 "
-                          f"cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+                "sample": f"first {cells} of {n} cells x {hs} host steps of {w.dt:g} s, OpenMP static chunks of "
+                          f"{args.cpu_chunk} cells, OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
                           f"OMP_PLACES={os.environ.get('OMP_PLACES')}",
                 "seconds": el,
                 "attempts_per_cell_solve_sample": float(att[:cells].sum()) / (cells * hs),

@@ -205,7 +205,7 @@ class RefSolver:
         self.np_ = self.lib.mkpp_ref_num_parameters()
 
     def integrate(self, conc, dt, steps=1, temp=None, rho=None, rh=None, clw=None, param=None, nthreads=0,
-                  seed=None, **_):
+                  seed=None, chunk=64, **_):
         conc = np.ascontiguousarray(conc, dtype=np.float64)
         n = conc.shape[1]
         full = lambda a, v: np.ascontiguousarray(np.full(n, v) if a is None else a, dtype=np.float64)  # noqa: E731
@@ -216,7 +216,7 @@ class RefSolver:
                                          vp(CLW.ctypes.data), vp(RHO.ctypes.data), vp(P.ctypes.data),
                                          C.c_int(P.shape[0]),
                                          C.c_double(dt), C.c_int(steps), C.c_int(nthreads),
-                                         C.c_double(-1.0 if seed is None else seed))
+                                         C.c_double(-1.0 if seed is None else seed), C.c_int(chunk))
         return {"conc": conc, "status": np.zeros(n, np.int32), "rc": rc}
 
     def evaluate(self, conc, temp=None, rho=None, rh=None, param=None, clw=None, **_):

@@ -76,15 +76,19 @@ int mkpp_ref_num_parameters() { return Solver::NUM_RUNTIME_PARAMETERS; }
 
 // conc[s * ncells + c] (in/out), param[p * ncells + c] with nparam rows; clw
 // (cloud liquid water, cloud-gated mechanisms only) may be null for 0.
+// chunk: cells per static OpenMP chunk, 64 as the reference's
+// RangePolicy(0, cells, ChunkSize(64)); a smaller chunk keeps every thread
+// busy on a sample of fewer than 64 cells per thread.
 int mkpp_ref_integrate(int ncells, double* conc, const double* temp, const double* rh, const double* clw,
                        const double* rho, const double* param, int nparam, double dt, int steps, int nthreads,
-                       double seed) {
+                       double seed, int chunk) {
   if (nthreads > 0) omp_set_num_threads(nthreads);
   const int np = Solver::NUM_RUNTIME_PARAMETERS > 0 ? Solver::NUM_RUNTIME_PARAMETERS : 1;
+  if (chunk < 1) chunk = 64;
 #pragma omp parallel
   {
     std::vector<double> forcing(np, 0.0);
-#pragma omp for schedule(static, 64)
+#pragma omp for schedule(static, chunk)
     for (int c = 0; c < ncells; ++c) {
       Solver solver;
       if (seed > 0.0) solver.initial_step_seed = seed;
