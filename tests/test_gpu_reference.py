@@ -25,7 +25,8 @@ from mkpp_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
 
-CELLS = {"chapman": 512, "small_strato": 512, "saprc99": 48, "chapman_rodas3": 512, "small_strato_rodas3": 512}
+CELLS = {"chapman": 512, "small_strato": 512, "saprc99": 48, "chapman_rodas3": 512, "small_strato_rodas3": 512,
+         "ts1": 32}
 
 
 def _run(mech):
@@ -66,3 +67,19 @@ def test_free_running_matches_reference_solver_saprc99(built_libs):
     rel = np.abs(got - ref)[:, ok] / np.maximum(np.abs(ref[:, ok]), 1.0)
     assert np.median(rel) <= 1e-9
     assert rel.max() <= 1e-2
+
+
+def test_free_running_matches_reference_solver_ts1():
+    """TS1 (table-driven library) against the reference's own TS1 solver at
+    the plan's tolerances, 32 cells over one 600 s host step, with the
+    shipped 1e29-1e41 1/s rates: every cell finite on both sides, every
+    species within 10 (rtol |ref| + atol), the median relative difference
+    (|ref| + atol) at most 1e-9."""
+    from mkpp_gb300 import build
+
+    build.build(("ts1",))
+    got, ref, ok, rtol, atol = _run("ts1")
+    assert ok.all()
+    d = np.abs(got - ref)
+    assert np.all(d <= 10 * (rtol * np.abs(ref) + atol))
+    assert np.median(d / (np.abs(ref) + atol)) <= 1e-9

@@ -118,6 +118,30 @@ def test_integrate_matches_reference_statistically(mech):
     assert np.all(ro["status"][bad_ref] != 0)
 
 
+def test_ts1_integrate_matches_reference():
+    """TS1 integrate() over one 600 s host step against the reference's own
+    solver regenerated at the plan's tolerances (rtol 1e-3, atol 1 molec/cm3
+    in mol/m3), 32 seeded cells.  Its six Troe rate constants of 1e29-1e41
+    1/s make the trajectory depend on rounding, as for SAPRC99, so the bound
+    is statistical and in the tolerance's units: median relative difference
+    (|ref| + atol) below 1e-9 and every species of every cell within
+    10 (rtol |ref| + atol), the bound of the free-running GPU tests
+    (measured 1.7e-11 and 7.6)."""
+    ref = _ref("ts1")
+    o = Oracle("ts1")
+    w = workloads.make("ts1", 32)
+    P = w.param_at(0)
+    ro = o.integrate(w.conc.copy(), w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P)
+    rr = ref.integrate(w.conc.copy(), w.dt, 1, temp=w.temp, rho=w.rho, rh=w.rh, param=P, chunk=1)
+    both = (ro["status"] == 0) & np.isfinite(rr["conc"]).all(axis=0)
+    assert both.all()
+    atol = np.array(o.raw["atol"])[:, None]
+    rtol = np.array(o.raw["rtol"])[:, None]
+    d = np.abs(ro["conc"] - rr["conc"])
+    assert np.median(d / (np.abs(rr["conc"]) + atol)) < 1e-9
+    assert np.all(d <= 10 * (rtol * np.abs(rr["conc"]) + atol))
+
+
 # ---------------------------------------------------------------------------
 # TS1 (210 species, 547 reactions, 547 runtime parameters).  Pinned at the
 # tendency and Jacobian level against fixtures of the reference's own
