@@ -1,12 +1,14 @@
 """The allocation-free integrate entry point (mkpp_gpu_integrate_noalloc).
 
-Some callers cannot allocate device memory where they integrate, e.g. a host
-model recording its time step into a CUDA graph, where cudaMalloc is not
-allowed during capture.  This entry point keeps its scratch in a static device
-array of the library.  The test calls it through the C ABI and checks it
-against the workspace-based entry point on the same inputs, on two calls in a
-row (the second call reuses the array the first one left behind).  It is
-collected last so that a failure here comes after every other test has run.
+Some host models must not allocate device memory where they call the
+chemistry: their own pool allocator owns the free device memory, or their
+time loop avoids cudaMalloc/cudaFree because those synchronise the whole
+device.  This entry point keeps its scratch in a static device array of the
+library instead.  The test calls it through the C ABI on two calls in a row
+and checks each against the workspace-based entry point on the same inputs:
+the second call takes other cells than the first, so a result that leaned on
+what the first call left in the shared array would differ.  It is collected
+last so that a failure here comes after every other test has run.
 """
 import ctypes as C
 
@@ -25,32 +27,35 @@ def test_noalloc_matches_workspace_entry_point(built_libs):
     lib = load_library("saprc99")
     s = DeviceSolver("saprc99")
     n = 512
-    w = workloads.make("saprc99", n)
+    w = workloads.make("saprc99", 2 * n)
     d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
-    conc0 = d(w.conc)
-    ktab, st0 = s.rate_constants(conc0, d(w.temp), d(w.rho), d(w.rh), None, d(w.param))
-    torch.cuda.synchronize()
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-
-    # Existing entry point (plain form, caller-provided workspace).
-    ref = conc0.clone()
-    rst = st0.clone()
-    racc = torch.zeros(n, dtype=torch.int32, device="cuda")
-    rrej = torch.zeros_like(racc)
-    s.integrate_k(ref, ktab, w.dt, mode="plain", status=rst, accepted=racc, rejected=rrej)
-    torch.cuda.synchronize()
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
 
     for call in range(2):
+        cells = slice(call * n, (call + 1) * n)
+        conc0 = d(w.conc[:, cells])
+        ktab, st0 = s.rate_constants(conc0, d(w.temp[cells]), d(w.rho[cells]), d(w.rh[cells]), None,
+                                     d(w.param[:, cells]))
+        torch.cuda.synchronize()
+
+        # Existing entry point (plain form, caller-provided workspace).
+        ref = conc0.clone()
+        rst = st0.clone()
+        racc = torch.zeros(n, dtype=torch.int32, device="cuda")
+        rrej = torch.zeros_like(racc)
+        s.integrate_k(ref, ktab, w.dt, mode="plain", status=rst, accepted=racc, rejected=rrej)
+        torch.cuda.synchronize()
+
         out = conc0.clone()
         ost = st0.clone()
         oacc = torch.zeros(n, dtype=torch.int32, device="cuda")
         orej = torch.zeros_like(oacc)
-        rc = lib.mkpp_gpu_integrate_noalloc(
-            C.c_size_t(n), C.c_void_p(out.data_ptr()), C.c_void_p(ktab.data_ptr()), C.c_size_t(0), 1,
-            C.c_double(w.dt), C.c_double(s.default_seed), 20000, C.c_void_p(ost.data_ptr()),
-            C.c_void_p(oacc.data_ptr()), C.c_void_p(orej.data_ptr()), stream)
+        rc = lib.mkpp_gpu_integrate_noalloc(C.c_size_t(n), p(out), p(ktab), C.c_size_t(0), 1, C.c_double(w.dt),
+                                            C.c_double(s.default_seed), 20000, p(ost), p(oacc), p(orej), stream)
         assert rc == 0, rc
         torch.cuda.synchronize()
+        # Bit for bit (a non-finite cell compares as non-finite on both sides).
         assert torch.equal(torch.nan_to_num(out, nan=1.25e300), torch.nan_to_num(ref, nan=1.25e300)), f"call {call}"
         assert torch.equal(ost, rst) and torch.equal(oacc, racc) and torch.equal(orej, rrej), f"call {call}"
 
