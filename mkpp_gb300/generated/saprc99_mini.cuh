@@ -672,7 +672,7 @@ struct Mech {
   // Mass-action tendencies F(y) of the variable species (logical order):
   // y(i) supplies the state, out(i, F_i) receives the result.
   template <class YA, class KA, class FO>
-  __device__ __forceinline__ static void fun(const YA& y, const KA& k, FO&& out) {
+  __device__ __noinline__ static void fun(const YA& y, const KA& k, FO&& out) {
     const double y2 = y(2);
     const double y3 = y(3);
     const double y4 = y(4);
@@ -716,7 +716,7 @@ struct Mech {
 
   // W = I/(gamma h) - J(y) into the LU slots that hold W entries.
   template <class YA, class KA, class SA>
-  __device__ __forceinline__ static void jac_w(const YA& y, const KA& k, double inv_g_dt, SA& S) {
+  __device__ __noinline__ static void jac_w(const YA& y, const KA& k, double inv_g_dt, SA& S) {
     (void)inv_g_dt;
     const double y3 = y(3);
     const double y6 = y(6);
@@ -868,7 +868,7 @@ struct Mech {
   // entries for the U part, the pivot column of U for the L part) are read
   // once into registers.  Diagonal slots end up holding 1/U_ii.
   template <class SA>
-  __device__ __forceinline__ static bool factor(SA& S) {
+  __device__ __noinline__ static bool factor(SA& S) {
     bool ok = true;
     {  // pivot row 0
       const double u0 = S[0];
@@ -1078,7 +1078,7 @@ struct Mech {
   // Solve (LU) x = b in place on slots [base, base + NV): unit-L forward
   // sweep, then the U backward sweep scaled by the stored 1/U_ii.
   template <class SA>
-  __device__ __forceinline__ static void solve(SA& S, const int base) {
+  __device__ __noinline__ static void solve(SA& S, const int base) {
     const double v0 = S[base + 0];
     const double v1 = S[base + 1];
     const double v2 = S[base + 2];

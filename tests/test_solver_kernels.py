@@ -102,16 +102,20 @@ def test_without_gpu_the_first_solve_fails_loudly(tmp_path):
     assert "FATAL ERROR" in out.stderr
 
 
+# TS1 runs 4 cells over 60 s: its synchronous form solves one cell per
+# call, each on a single lane of the table-driven attempt.
 @pytest.mark.gpu
-@pytest.mark.parametrize("mech,n,steps", [("chapman", 256, 2), ("small_strato", 256, 2), ("saprc99", 64, 1),
-                                          ("ts1", 32, 1)])
-def test_solver_kernels_match_c_abi(mech, n, steps, tmp_path):
+@pytest.mark.parametrize("mech,n,steps,dt", [("chapman", 256, 2, None), ("small_strato", 256, 2, None),
+                                             ("saprc99", 64, 1, None), ("ts1", 4, 1, 60.0)])
+def test_solver_kernels_match_c_abi(mech, n, steps, dt, tmp_path):
     from mkpp_gb300 import build
     from mkpp_gb300.api import MechanismContext
 
     build.build((mech,))
     exe = _compile(mech, tmp_path)
     w = _inputs(mech, n, tmp_path)
+    if dt is not None:
+        w.dt = dt
     out = subprocess.run([str(exe), str(tmp_path), str(n), repr(w.dt), str(steps)], capture_output=True, text=True,
                          env={**os.environ, "MKPP_GB300_LIB_DIR": str(LIB)})
     assert out.returncode == 0, out.stderr
