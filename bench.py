@@ -312,6 +312,8 @@ def cpu_runner(mechanism: str):
         from oracle import ref_build
 
         ref = ref_build.load(mechanism)
+        if ref is None and mechanism in ref_build.ON_DEMAND + tuple(ref_build.VARIANTS):
+            ref = ref_build.ensure(mechanism)   # compiled here from its generated headers
     except Exception:
         ref = None
     if ref is not None:
@@ -325,7 +327,7 @@ def cpu_integrate(runner, sub, conc, first: int, last: int, threads: int, chunk:
     """Host steps [first, last) of every cell of `sub`, in place on conc;
     returns the seconds.  One OpenMP parallel region per host step, as the
     reference's host loop calls its dispatcher once per host step."""
-    extra = {"chunk": chunk} if chunk != 64 else {}
+    extra = {"chunk": chunk} if chunk != 64 and hasattr(runner, "np_") else {}
     params = [sub.param_at(s) for s in range(first, last)]
     t0 = time.perf_counter()
     for par in params:
