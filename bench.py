@@ -102,6 +102,10 @@ def parse():
     ap.add_argument("--bulk-defer", type=int, default=0,
                     help="park each cell for the warp-cooperative kernel after this many attempts (0: never); "
                          "1 with few cells measures the cooperative kernel's attempt latency")
+    ap.add_argument("--split", default="auto",
+                    help="split launch of the window (mkpp_set_split_launch): 'auto' plans it from the first "
+                         "warm-up window's attempt counts and keeps it only if a warm-up window with it beats one "
+                         "without, 'off', or CELLS:BLOCKS")
     ap.add_argument("--bulk-only", action="store_true",
                     help="run only the bulk-rate section (a small case for profilers) and print its JSON")
     return ap.parse_args()
@@ -299,6 +303,36 @@ def adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, window_ms) ->
     return out
 
 
+def split_plan(att, grid_blocks: int, t_lane: float, t_warp: float, warps_per_block: int = 4):
+    """(cells, blocks, modelled seconds) of the split launch for a window
+    whose cells need `att` attempts each (the previous window's counts).
+    Cells are handed out most expensive first.  Model: the first `cells`
+    cells run on blocks x warps_per_block whole warps at t_warp seconds per
+    attempt, while the persistent kernel, with `blocks` fewer blocks of 128
+    lanes, runs the rest at t_lane seconds per attempt per lane (all lanes
+    busy); each side ends when its total work is done or its largest cell
+    is, whichever is later.  (0, 0, t) is the launch without the split."""
+    c = np.sort(np.asarray(att, dtype=np.float64))[::-1]
+    pre = np.concatenate([[0.0], np.cumsum(c)])
+    total = pre[-1]
+    lanes0 = grid_blocks * 128
+    best = (0, 0, max(total * t_lane / lanes0, c[0] * t_lane))
+    ks = np.unique(np.concatenate([np.arange(0, min(len(c), 256)), np.geomspace(256, len(c), 64).astype(int)]))
+    ks = ks[(ks > 0) & (ks < len(c))]
+    for blocks in (2, 4, 8, 16, 24, 32, 48):
+        if blocks >= grid_blocks:
+            break
+        warps = blocks * warps_per_block
+        lanes = (grid_blocks - blocks) * 128
+        coop = np.maximum(pre[ks] * t_warp / warps, c[0] * t_warp)
+        lane = np.maximum((total - pre[ks]) * t_lane / lanes, c[ks] * t_lane)
+        span = np.maximum(coop, lane)
+        j = int(np.argmin(span))
+        if span[j] < best[2]:
+            best = (int(ks[j]), blocks, float(span[j]))
+    return best
+
+
 def cpu_sample_cells(args, threads: int) -> int:
     """Cells of the CPU sample: at least 4096, and at least one 64-cell chunk
     of the reference's static OpenMP schedule per thread."""
@@ -483,15 +517,75 @@ def main():
         if args.order:
             order.copy_(torch.argsort(acc + rej, descending=True).to(torch.int32))
 
+    # Split launch: planned from the first warm-up window's attempt counts
+    # with the per-attempt times of a lane (all lanes busy) and of a whole
+    # warp, both measured here on capped cells; kept only if a warm-up
+    # window with it beats one without (same cost order).
+    split = (0, 0)
+    split_info = {"mode": args.split}
+    if args.split not in ("auto", "off"):
+        split = tuple(int(x) for x in args.split.split(":"))
+    t_lane = t_warp = None
+    if args.split == "auto" and args.order and args.warmup >= 2:
+        defer_default = int(os.environ.get("MKPP_DEFER_AFTER", "3000"))
+        blocks_env = int(os.environ.get("MKPP_BLOCKS_PER_SM", "0"))
+        b_lane = bulk_rate(w.mechanism, min(n, 77824), 20, stream)
+        b_warp = bulk_rate(w.mechanism, 152, 40, stream, defer=1)
+        solver.set_tuning(0, blocks_env, defer_default)
+        # 39 of the 40 attempts run on a warp; x1.3 for sharing the SM with
+        # a persistent block.
+        t_warp = 1.3 * b_warp["ms"] * 1e-3 / 39.0
+        split_info.update(t_warp_s=t_warp, bulk_attempts_per_s=b_lane["attempts_per_s"])
+
     # Warm-up windows, eager, with events around the integrate launch.
     ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     kernel_ms = []
+    timed_cfg_ms = []      # warm-up windows run with the configuration that is timed
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
+            if args.split == "auto" and t_warp is not None:
+                if i == 1:
+                    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+                    # resident blocks of 128 lanes: 2 per SM for the 255-register
+                    # variant, 4 for the 128-register one (or the cap set)
+                    per_sm = 4 if os.environ.get("MKPP_REGISTER_VARIANT") == "4" else 2
+                    if int(os.environ.get("MKPP_BLOCKS_PER_SM", "0")) > 0:
+                        per_sm = min(per_sm, int(os.environ["MKPP_BLOCKS_PER_SM"]))
+                    grid_blocks = per_sm * sms
+                    lanes = grid_blocks * 128
+                    t_lane = lanes / split_info["bulk_attempts_per_s"]
+                    k, b, span = split_plan((acc + rej).cpu().numpy(), grid_blocks, t_lane, t_warp)
+                    split = (k, b)
+                    split_info.update(grid_blocks=grid_blocks, t_lane_s=t_lane, planned=[k, b],
+                                      modelled_ms=span * 1e3)
+                    solver.set_split_launch(*split)
+                elif i == 2:
+                    solver.set_split_launch(0, 0)
+                elif i == 3:
+                    use = split != (0, 0) and kernel_ms[1] < kernel_ms[2]
+                    split_info["kept"] = bool(use)
+                    if not use:
+                        split = (0, 0)
+                    solver.set_split_launch(*split)
+                    timed_cfg_ms = [kernel_ms[1] if use else kernel_ms[2]]
+            elif i == 0 and split != (0, 0):
+                solver.set_split_launch(*split)
             window(ev)
             stream.synchronize()
             kernel_ms.append(ev[0].elapsed_time(ev[1]))
-            log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms")
+            if i >= 3 or (args.split != "auto" and i >= 1):
+                timed_cfg_ms.append(kernel_ms[-1])
+            log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms (split {split})")
+        if args.split == "auto" and t_warp is not None and args.warmup == 3:
+            use = split != (0, 0) and kernel_ms[1] < kernel_ms[2]
+            split_info["kept"] = bool(use)
+            if not use:
+                split = (0, 0)
+            solver.set_split_launch(*split)
+            timed_cfg_ms = [kernel_ms[1] if use else kernel_ms[2]]
+    split_info["cells_blocks"] = list(split)
+    if not timed_cfg_ms:
+        timed_cfg_ms = kernel_ms[1:] or kernel_ms
     # Capture the window: hs rate-constant launches, the persistent integrate
     # launch and, with parking enabled, the cooperative launch (which finds no
     # parked cell: no cell of a 24-step window reaches 24 x 3000 attempts).
@@ -512,6 +606,7 @@ def main():
     barrier(world)
     el_ms = max_over_ranks(start.elapsed_time(end), world) / args.steps
     log(f"timed: {el_ms:.0f} ms per window")
+    solver.set_split_launch(0, 0)   # the later sections run without it
     clk = clocks.summary()
     cell_solves = shard.sum_over_ranks(n * hs)
     value = cell_solves / (el_ms * 1e-3)
@@ -522,7 +617,7 @@ def main():
     attempts = int(att.sum())
     fpa = flops_per_attempt(plan)
     flops_run = attempts * fpa["total"]
-    kernel_avg_ms = statistics.mean(kernel_ms[1:] or kernel_ms) if kernel_ms else float("nan")
+    kernel_avg_ms = statistics.mean(timed_cfg_ms) if kernel_ms else float("nan")
     achieved = flops_run / (kernel_avg_ms * 1e-3) / 1e12 if kernel_ms else None
 
     # Live FP64 FMA peak (DFMA probe on this GPU).
@@ -548,12 +643,12 @@ def main():
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
         "gpu_launches": args.steps * (hs + 1 + (int(os.environ.get("MKPP_DEFER_AFTER", "3000")) > 0
-                                                or args.tail_after > 0)),
+                                                or args.tail_after > 0) + (split != (0, 0))),
         "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
                    "defer_after_per_host_step": os.environ.get("MKPP_DEFER_AFTER", "3000"), "cost_order": bool(args.order),
                    "tail_after": args.tail_after,
-                   "max_attempts_per_call": args.max_attempts},
+                   "max_attempts_per_call": args.max_attempts, "split": split_info},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
                  "attempts_per_cell_window_pct": {q: float(np.percentile(att, q)) for q in (50, 90, 99, 100)},

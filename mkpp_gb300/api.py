@@ -88,6 +88,7 @@ SIGNATURES = [
     ("mkpp_gpu_integrate_replay", _i, [_sz, _vp, _vp, _i, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_gpu_adjoint", _i, [_sz, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("mkpp_set_cost_order", _i, [_vp, _i]),
+    ("mkpp_set_split_launch", _i, [_i, _i]),
     ("mkpp_set_dt_carryover", _i, [_vp, _i]),
     ("mkpp_gpu_integrate_carry", _i, [_sz, _vp, _vp, _sz, _i, _d, _d, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
                                       _vp]),
@@ -310,6 +311,12 @@ class DeviceSolver:
     def set_tuning(self, register_variant=0, blocks_per_sm=0, defer_after=-1):
         self._check(self.lib.mkpp_set_launch_tuning(C.c_int(register_variant), C.c_int(blocks_per_sm),
                                                     C.c_int(defer_after)))
+        self._ws = None
+
+    def set_split_launch(self, cells: int, blocks: int):
+        """The first `cells` entries of a launch's cell order go to `blocks`
+        blocks of whole warps beside the persistent kernel (0: off)."""
+        self._check(self.lib.mkpp_set_split_launch(C.c_int(cells), C.c_int(blocks)))
         self._ws = None
 
     def set_tail_parking(self, min_attempts: int):

@@ -130,6 +130,11 @@ struct Tuning {
   int blocks_per_sm = 0;
   int defer_after = kDefaultDeferPerStep;
   int tail_after = 0;  // tail parking threshold in attempts (0: off)
+  // Split launch (mkpp_set_split_launch): with a cell order, its first
+  // split_cells cells go to split_blocks blocks of whole warps beside the
+  // persistent kernel (0: off).
+  int split_cells = 0;
+  int split_blocks = 0;
 };
 
 Tuning& tuning() {
@@ -151,6 +156,7 @@ struct LaunchConfig {
   int coop_warps = 0;
   size_t coop_smem = 0;
   bool coop_ok = false;
+  bool split_ok = false;
 };
 
 template <int MINB>
@@ -181,8 +187,35 @@ const LaunchConfig& launch_config() {
     cfg.coop_warps = (int)std::min<size_t>(mkpp::kCoopWarps, (200u * 1024u) / per_warp);
     cfg.coop_smem = per_warp * (size_t)std::max(1, cfg.coop_warps);
     cfg.coop_ok = cfg.coop_warps >= 1 && set_coop_smem(cfg.coop_smem) == MKPP_SUCCESS;
+    cfg.split_ok = cfg.coop_ok && set_split_smem(cfg.coop_smem) == MKPP_SUCCESS;
   }
   return cfg;
+}
+
+// Side stream and fork/join events of the split launch, one set per device,
+// created by the first split launch on that device (make it before any
+// stream capture).
+struct SplitStreams {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+int split_streams(SplitStreams** out) {
+  static std::mutex m;
+  static SplitStreams per_device[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MKPP_ERROR_DEVICE;
+  std::lock_guard<std::mutex> lock(m);
+  SplitStreams& s = per_device[dev];
+  if (!s.side) {
+    if (cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) {
+      return MKPP_ERROR_DEVICE;
+    }
+  }
+  *out = &s;
+  return MKPP_SUCCESS;
 }
 
 int integrate_grid() { return launch_config().grid; }
@@ -221,9 +254,24 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   a.active = (unsigned int*)ws + 2;
   double* scratch = StoreInfo::block_bytes ? (double*)(ws + scratch_offset()) : nullptr;
   const LaunchConfig& cfg = launch_config();
-  if (cudaMemsetAsync(ws, 0, 3 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
+  if (cudaMemsetAsync(ws, 0, 4 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
   if (mode == 1) {
     const Tuning& t = tuning();
+    // Split launch: the order's first cells on whole warps beside the
+    // persistent kernel, which leaves their blocks' SM resources free.
+    int grid = cfg.grid;
+    SplitStreams* ss = nullptr;
+    if (t.split_cells > 0 && t.split_blocks > 0 && a.order && cfg.split_ok && cfg.grid > t.split_blocks) {
+      if (split_streams(&ss) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      a.split_cells = (int)std::min<long long>(t.split_cells, a.ncells);
+      a.split_next = (unsigned int*)ws + 3;
+      grid = cfg.grid - t.split_blocks;
+      if (cudaEventRecord(ss->fork, stream) != cudaSuccess || cudaStreamWaitEvent(ss->side, ss->fork, 0) != cudaSuccess)
+        return MKPP_ERROR_DEVICE;
+      if (launch_split(a, t.split_blocks, cfg.coop_warps * 32, cfg.coop_smem, ss->side) != MKPP_SUCCESS)
+        return MKPP_ERROR_DEVICE;
+      if (cudaEventRecord(ss->join, ss->side) != cudaSuccess) return MKPP_ERROR_DEVICE;
+    }
     const long long park = (long long)t.defer_after * std::max(1, a.steps);
     a.defer_after = (int)std::min<long long>(park, INT32_MAX);
     // Tail parking runs in the 255-register variant only.
@@ -233,12 +281,13 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
     if (tail && a.defer) {
       a.tail_after = t.tail_after;
       a.tail_cells = (unsigned)(cfg.sms * 2 * cfg.coop_warps);
-      if (launch_persistent_tail(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      if (launch_persistent_tail(a, scratch, grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else if (cfg.minb == 4) {
-      if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      if (launch_persistent4(a, scratch, grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else {
-      mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+      mkpp::integrate_persistent_kernel<Mech, 2><<<grid, mkpp::kBlock, 0, stream>>>(a, scratch);
     }
+    if (ss && cudaStreamWaitEvent(stream, ss->join, 0) != cudaSuccess) return MKPP_ERROR_DEVICE;
     if (a.defer) {
       if (launch_coop(a, cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream) != MKPP_SUCCESS) {
         return MKPP_ERROR_DEVICE;
@@ -800,6 +849,14 @@ size_t mkpp_gpu_workspace_bytes(size_t num_cells) { return workspace_bytes(num_c
 int mkpp_set_tail_parking(int min_attempts) {
   if (min_attempts < 0) return MKPP_ERROR_INVALID_ARGUMENT;
   tuning().tail_after = min_attempts;
+  return MKPP_SUCCESS;
+}
+
+int mkpp_set_split_launch(int split_cells, int split_blocks) {
+  if (split_cells < 0 || split_blocks < 0) return MKPP_ERROR_INVALID_ARGUMENT;
+  Tuning& t = tuning();
+  t.split_cells = split_cells;
+  t.split_blocks = split_blocks;
   return MKPP_SUCCESS;
 }
 

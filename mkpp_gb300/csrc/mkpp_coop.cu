@@ -1,6 +1,6 @@
-// The warp-cooperative integrate of parked cells for one mechanism library,
-// in its own translation unit so it compiles in parallel with the other
-// kernels.
+// The warp-cooperative integrate of parked cells, and the split form's
+// warp-cooperative kernel, for one mechanism library, in their own
+// translation unit so they compile in parallel with the other kernels.
 #include "capi_common.cuh"
 
 namespace mkpp_tu {
@@ -14,6 +14,18 @@ int set_coop_smem(size_t bytes) {
 
 int launch_coop(const mkpp::LaunchArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
   mkpp::integrate_coop_kernel<Mech><<<grid, threads, smem, stream>>>(a);
+  return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
+}
+
+int set_split_smem(size_t bytes) {
+  return cudaFuncSetAttribute(mkpp::integrate_split_kernel<Mech>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes) == cudaSuccess
+             ? MKPP_SUCCESS
+             : MKPP_ERROR_DEVICE;
+}
+
+int launch_split(const mkpp::LaunchArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
+  mkpp::integrate_split_kernel<Mech><<<grid, threads, smem, stream>>>(a);
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
 

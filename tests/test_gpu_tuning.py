@@ -86,3 +86,43 @@ def test_tail_parking_leaves_results_unchanged(built_libs, mech):
         s.set_tail_parking(0)
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.parametrize("mech", ["small_strato", "saprc99"])
+def test_split_launch_leaves_results_unchanged(built_libs, mech):
+    """mkpp_set_split_launch: the first cells of the order on whole warps
+    beside the persistent kernel (a window of 2 host steps, 640 cells, the
+    order reversed, its first 40 cells on 4 blocks).  State, status, attempt
+    counts and carried step sizes end bit-identical to the launch without
+    the split, with and without step-size carry-over."""
+    import torch
+
+    from mkpp_gb300.api import DeviceSolver
+
+    n = 640
+    w, s = workloads.make(mech, n), DeviceSolver(mech)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    conc0 = d(w.conc)
+    nr = s.sizes.reactions
+    ktab = torch.empty((2, nr, n), dtype=torch.float64, device="cuda")
+    for h in range(2):
+        k, _ = s.rate_constants(conc0, d(w.temp), d(w.rho), d(w.rh), None, d(w.param_at(h)))
+        ktab[h].copy_(k)
+    order = torch.arange(n - 1, -1, -1, dtype=torch.int32, device="cuda")
+    for carry in (False, True):
+        outs = []
+        try:
+            for split in ((0, 0), (40, 4)):
+                s.set_split_launch(*split)
+                conc = conc0.clone()
+                st = torch.zeros(n, dtype=torch.int32, device="cuda")
+                acc, rej = torch.zeros_like(st), torch.zeros_like(st)
+                dtc = torch.zeros(n, dtype=torch.float64, device="cuda") if carry else None
+                s.integrate_k(conc, ktab, w.dt, steps=2, k_step_stride=nr * n, status=st, accepted=acc,
+                              rejected=rej, order=order, dt_carry=dtc)
+                torch.cuda.synchronize()
+                outs.append([x.cpu().numpy() for x in (conc, st, acc, rej) + ((dtc,) if carry else ())])
+        finally:
+            s.set_split_launch(0, 0)
+        for a, b in zip(outs[0], outs[1]):
+            assert np.array_equal(a, b, equal_nan=True)
