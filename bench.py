@@ -46,6 +46,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "SAPRC99 cell-solves/s on 1 GB300 at rtol 1e-3"
 
+# DRAM read + write bytes of integrate_persistent_kernel per attempt, from one
+# ncu capture of the capped case (python bench.py --bulk-only --bulk-cells
+# 19456 --bulk-attempts 20): 32.79 GB over 389120 attempts.
+DRAM_BYTES_PER_ATTEMPT = {"saprc99": 84.3e3}
+
 
 def metric_for(mechanism: str) -> str:
     """The metric's name for a workload: METRIC itself for SAPRC99, the same
@@ -662,10 +667,13 @@ def main():
             "peak_source": "measured live: DFMA probe (csrc/probe.cu) on this GPU",
             "kernel": "integrate_persistent_kernel", "launch_ms_avg": kernel_avg_ms,
             "algorithmic_flops_per_launch": flops_run,
-            # No DRAM capture of this build at this size; the last ncu capture
-            # (an earlier build, capped case) read+wrote 97 KB per attempt,
-            # about a quarter of HBM bandwidth at the FP64-bound attempt rate.
-            "traffic": None,
+            # DRAM bytes of the integrate kernel per launch: the ncu capture of
+            # the capped case (19456 cells x 20 attempts, dram__bytes_read +
+            # dram__bytes_write per attempt) scaled by this window's attempts.
+            "traffic": (attempts * DRAM_BYTES_PER_ATTEMPT[w.mechanism]
+                        if w.mechanism in DRAM_BYTES_PER_ATTEMPT else None),
+            "traffic_unit": "bytes per launch",
+            "traffic_source": "ncu, capped case, scaled by attempts (profiles/integrate_persistent_saprc99.md)",
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
         },
     }
