@@ -110,7 +110,7 @@ def parse():
     ap.add_argument("--split", default="auto",
                     help="split launch of the window (mkpp_set_split_launch): 'auto' plans it from the first "
                          "warm-up window's attempt counts and keeps it only if a warm-up window with it beats one "
-                         "without, 'off', or CELLS:BLOCKS")
+                         "without, 'off', or CELLS:SMS")
     ap.add_argument("--bulk-only", action="store_true",
                     help="run only the bulk-rate section (a small case for profilers) and print its JSON")
     return ap.parse_args()
@@ -308,33 +308,33 @@ def adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, window_ms) ->
     return out
 
 
-def split_plan(att, grid_blocks: int, t_lane: float, t_warp: float, warps_per_block: int = 4):
-    """(cells, blocks, modelled seconds) of the split launch for a window
-    whose cells need `att` attempts each (the previous window's counts).
-    Cells are handed out most expensive first.  Model: the first `cells`
-    cells run on blocks x warps_per_block whole warps at t_warp seconds per
-    attempt, while the persistent kernel, with `blocks` fewer blocks of 128
-    lanes, runs the rest at t_lane seconds per attempt per lane (all lanes
-    busy); each side ends when its total work is done or its largest cell
-    is, whichever is later.  (0, 0, t) is the launch without the split."""
+def split_plan(att, sms: int, t_lane: float, t_warp: float, blocks_per_sm: int = 2, warps_per_block: int = 4):
+    """(cells, reserved SMs, modelled seconds) of the split launch for a
+    window whose cells need `att` attempts each (the previous window's
+    counts).  Cells are handed out most expensive first.  Model: the first
+    `cells` cells run on the whole warps of the reserved SMs at t_warp
+    seconds per attempt, the rest on the lanes of the other SMs at t_lane
+    seconds per attempt per lane (all lanes busy); each side ends when its
+    total work is done or its largest cell is, whichever is later.  (0, 0, t)
+    is the launch without the split."""
     c = np.sort(np.asarray(att, dtype=np.float64))[::-1]
     pre = np.concatenate([[0.0], np.cumsum(c)])
     total = pre[-1]
-    lanes0 = grid_blocks * 128
-    best = (0, 0, max(total * t_lane / lanes0, c[0] * t_lane))
+    lanes_per_sm = blocks_per_sm * 128
+    best = (0, 0, max(total * t_lane / (sms * lanes_per_sm), c[0] * t_lane))
     ks = np.unique(np.concatenate([np.arange(0, min(len(c), 256)), np.geomspace(256, len(c), 64).astype(int)]))
     ks = ks[(ks > 0) & (ks < len(c))]
-    for blocks in (2, 4, 8, 16, 24, 32, 48):
-        if blocks >= grid_blocks:
+    for reserved in (1, 2, 4, 6, 8, 12, 16, 24, 32):
+        if reserved >= sms:
             break
-        warps = blocks * warps_per_block
-        lanes = (grid_blocks - blocks) * 128
+        warps = reserved * blocks_per_sm * warps_per_block
+        lanes = (sms - reserved) * lanes_per_sm
         coop = np.maximum(pre[ks] * t_warp / warps, c[0] * t_warp)
         lane = np.maximum((total - pre[ks]) * t_lane / lanes, c[ks] * t_lane)
         span = np.maximum(coop, lane)
         j = int(np.argmin(span))
         if span[j] < best[2]:
-            best = (int(ks[j]), blocks, float(span[j]))
+            best = (int(ks[j]), reserved, float(span[j]))
     return best
 
 
@@ -537,9 +537,8 @@ def main():
         b_lane = bulk_rate(w.mechanism, min(n, 77824), 20, stream)
         b_warp = bulk_rate(w.mechanism, 152, 40, stream, defer=1)
         solver.set_tuning(0, blocks_env, defer_default)
-        # 39 of the 40 attempts run on a warp; x1.3 for sharing the SM with
-        # a persistent block.
-        t_warp = 1.3 * b_warp["ms"] * 1e-3 / 39.0
+        # 39 of the 40 attempts run on a warp; x1.2 for 8 warps on an SM
+        t_warp = 1.2 * b_warp["ms"] * 1e-3 / 39.0
         split_info.update(t_warp_s=t_warp, bulk_attempts_per_s=b_lane["attempts_per_s"])
 
     # Warm-up windows, eager, with events around the integrate launch.
@@ -556,12 +555,10 @@ def main():
                     per_sm = 4 if os.environ.get("MKPP_REGISTER_VARIANT") == "4" else 2
                     if int(os.environ.get("MKPP_BLOCKS_PER_SM", "0")) > 0:
                         per_sm = min(per_sm, int(os.environ["MKPP_BLOCKS_PER_SM"]))
-                    grid_blocks = per_sm * sms
-                    lanes = grid_blocks * 128
-                    t_lane = lanes / split_info["bulk_attempts_per_s"]
-                    k, b, span = split_plan((acc + rej).cpu().numpy(), grid_blocks, t_lane, t_warp)
+                    t_lane = per_sm * sms * 128 / split_info["bulk_attempts_per_s"]
+                    k, b, span = split_plan((acc + rej).cpu().numpy(), sms, t_lane, t_warp, per_sm)
                     split = (k, b)
-                    split_info.update(grid_blocks=grid_blocks, t_lane_s=t_lane, planned=[k, b],
+                    split_info.update(sms=sms, t_lane_s=t_lane, planned_cells_sms=[k, b],
                                       modelled_ms=span * 1e3)
                     solver.set_split_launch(*split)
                 elif i == 2:
@@ -588,7 +585,7 @@ def main():
                 split = (0, 0)
             solver.set_split_launch(*split)
             timed_cfg_ms = [kernel_ms[1] if use else kernel_ms[2]]
-    split_info["cells_blocks"] = list(split)
+    split_info["cells_sms"] = list(split)
     if not timed_cfg_ms:
         timed_cfg_ms = kernel_ms[1:] or kernel_ms
     # Capture the window: hs rate-constant launches, the persistent integrate

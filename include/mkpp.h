@@ -157,17 +157,16 @@ int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_af
  * bit-identical.  Applies to the 255-register variant. */
 int mkpp_set_tail_parking(int min_attempts);
 /* Split launch (process-wide, default off; no reference counterpart): when
- * a persistent integrate launch has a cell_order, its first split_cells
- * cells are integrated by whole warps (split_blocks blocks of the
- * warp-cooperative kernel) on a side stream beside the persistent kernel,
- * which gives up those blocks and takes its cells from the rest of the
- * order.  A warp finishes an attempt of one cell about 3x sooner than a
- * lane, so the few most expensive cells, which otherwise set the end of the
- * launch, finish earlier.  Results are bit-identical.  The side stream and
- * its events are created by the first split launch on a device: make it
- * before any stream capture.  Give the cells in cost order (most expensive
- * first), e.g. the previous window's attempt counts. */
-int mkpp_set_split_launch(int split_cells, int split_blocks);
+ * a persistent integrate launch has a cell_order, the blocks on the first
+ * split_sms SMs integrate its first split_cells cells, each on a whole warp
+ * (the warp-cooperative attempt), while the other SMs run the persistent
+ * kernel's body over the rest of the order, in the same launch.  A warp on
+ * an SM that runs no lanes finishes an attempt of one cell about 3x sooner
+ * than a lane, so the few most expensive cells, which otherwise set the end
+ * of the launch, finish earlier.  Results are bit-identical.  Applies to the
+ * 255-register variant without tail parking.  Give the cells in cost order
+ * (most expensive first), e.g. the previous window's attempt counts. */
+int mkpp_set_split_launch(int split_cells, int split_sms);
 
 /* Rate constants of every reaction into ktab[cell + num_cells * reaction].
  * temp/rho/rh/clw/param may be NULL (compile-time environment, 0.5, 0, zeros).

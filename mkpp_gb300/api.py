@@ -313,10 +313,10 @@ class DeviceSolver:
                                                     C.c_int(defer_after)))
         self._ws = None
 
-    def set_split_launch(self, cells: int, blocks: int):
-        """The first `cells` entries of a launch's cell order go to `blocks`
-        blocks of whole warps beside the persistent kernel (0: off)."""
-        self._check(self.lib.mkpp_set_split_launch(C.c_int(cells), C.c_int(blocks)))
+    def set_split_launch(self, cells: int, sms: int):
+        """The first `cells` entries of a launch's cell order go to whole
+        warps on `sms` reserved SMs, in the persistent launch (0: off)."""
+        self._check(self.lib.mkpp_set_split_launch(C.c_int(cells), C.c_int(sms)))
         self._ws = None
 
     def set_tail_parking(self, min_attempts: int):

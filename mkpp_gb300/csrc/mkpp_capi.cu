@@ -131,10 +131,10 @@ struct Tuning {
   int defer_after = kDefaultDeferPerStep;
   int tail_after = 0;  // tail parking threshold in attempts (0: off)
   // Split launch (mkpp_set_split_launch): with a cell order, its first
-  // split_cells cells go to split_blocks blocks of whole warps beside the
-  // persistent kernel (0: off).
+  // split_cells cells go to whole warps on the first split_sms SMs, the
+  // persistent body runs on the others (0: off).
   int split_cells = 0;
-  int split_blocks = 0;
+  int split_sms = 0;
 };
 
 Tuning& tuning() {
@@ -192,32 +192,6 @@ const LaunchConfig& launch_config() {
   return cfg;
 }
 
-// Side stream and fork/join events of the split launch, one set per device,
-// created by the first split launch on that device (make it before any
-// stream capture).
-struct SplitStreams {
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
-};
-
-int split_streams(SplitStreams** out) {
-  static std::mutex m;
-  static SplitStreams per_device[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MKPP_ERROR_DEVICE;
-  std::lock_guard<std::mutex> lock(m);
-  SplitStreams& s = per_device[dev];
-  if (!s.side) {
-    if (cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) {
-      return MKPP_ERROR_DEVICE;
-    }
-  }
-  *out = &s;
-  return MKPP_SUCCESS;
-}
-
 int integrate_grid() { return launch_config().grid; }
 
 // Workspace layout: [queue counter, parked-cell counter, active-cell counter | 256 B]
@@ -257,20 +231,15 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
   if (cudaMemsetAsync(ws, 0, 4 * sizeof(unsigned int), stream) != cudaSuccess) return MKPP_ERROR_DEVICE;
   if (mode == 1) {
     const Tuning& t = tuning();
-    // Split launch: the order's first cells on whole warps beside the
-    // persistent kernel, which leaves their blocks' SM resources free.
-    int grid = cfg.grid;
-    SplitStreams* ss = nullptr;
-    if (t.split_cells > 0 && t.split_blocks > 0 && a.order && cfg.split_ok && cfg.grid > t.split_blocks) {
-      if (split_streams(&ss) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+    // Split launch: the order's first cells on whole warps on reserved SMs,
+    // in the same launch as the persistent body (255-register variant, a
+    // whole warp's store fitting the block's shared memory).
+    const bool split = t.split_cells > 0 && t.split_sms > 0 && t.split_sms < cfg.sms && a.order && cfg.split_ok &&
+                       cfg.minb == 2 && t.tail_after == 0 && cfg.coop_warps * 32 == mkpp::kBlock;
+    if (split) {
       a.split_cells = (int)std::min<long long>(t.split_cells, a.ncells);
+      a.split_sms = t.split_sms;
       a.split_next = (unsigned int*)ws + 3;
-      grid = cfg.grid - t.split_blocks;
-      if (cudaEventRecord(ss->fork, stream) != cudaSuccess || cudaStreamWaitEvent(ss->side, ss->fork, 0) != cudaSuccess)
-        return MKPP_ERROR_DEVICE;
-      if (launch_split(a, t.split_blocks, cfg.coop_warps * 32, cfg.coop_smem, ss->side) != MKPP_SUCCESS)
-        return MKPP_ERROR_DEVICE;
-      if (cudaEventRecord(ss->join, ss->side) != cudaSuccess) return MKPP_ERROR_DEVICE;
     }
     const long long park = (long long)t.defer_after * std::max(1, a.steps);
     a.defer_after = (int)std::min<long long>(park, INT32_MAX);
@@ -281,13 +250,14 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
     if (tail && a.defer) {
       a.tail_after = t.tail_after;
       a.tail_cells = (unsigned)(cfg.sms * 2 * cfg.coop_warps);
-      if (launch_persistent_tail(a, scratch, grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      if (launch_persistent_tail(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+    } else if (split) {
+      if (launch_split(a, scratch, cfg.grid, cfg.coop_smem, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else if (cfg.minb == 4) {
-      if (launch_persistent4(a, scratch, grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else {
-      mkpp::integrate_persistent_kernel<Mech, 2><<<grid, mkpp::kBlock, 0, stream>>>(a, scratch);
+      mkpp::integrate_persistent_kernel<Mech, 2><<<cfg.grid, mkpp::kBlock, 0, stream>>>(a, scratch);
     }
-    if (ss && cudaStreamWaitEvent(stream, ss->join, 0) != cudaSuccess) return MKPP_ERROR_DEVICE;
     if (a.defer) {
       if (launch_coop(a, cfg.sms * 2, cfg.coop_warps * 32, cfg.coop_smem, stream) != MKPP_SUCCESS) {
         return MKPP_ERROR_DEVICE;
@@ -852,11 +822,11 @@ int mkpp_set_tail_parking(int min_attempts) {
   return MKPP_SUCCESS;
 }
 
-int mkpp_set_split_launch(int split_cells, int split_blocks) {
-  if (split_cells < 0 || split_blocks < 0) return MKPP_ERROR_INVALID_ARGUMENT;
+int mkpp_set_split_launch(int split_cells, int split_sms) {
+  if (split_cells < 0 || split_sms < 0) return MKPP_ERROR_INVALID_ARGUMENT;
   Tuning& t = tuning();
   t.split_cells = split_cells;
-  t.split_blocks = split_blocks;
+  t.split_sms = split_sms;
   return MKPP_SUCCESS;
 }
 

@@ -24,8 +24,8 @@ int set_split_smem(size_t bytes) {
              : MKPP_ERROR_DEVICE;
 }
 
-int launch_split(const mkpp::LaunchArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
-  mkpp::integrate_split_kernel<Mech><<<grid, threads, smem, stream>>>(a);
+int launch_split(const mkpp::LaunchArgs& a, double* scratch, int grid, size_t smem, cudaStream_t stream) {
+  mkpp::integrate_split_kernel<Mech><<<grid, mkpp::kBlock, smem, stream>>>(a, scratch);
   return cudaGetLastError() == cudaSuccess ? MKPP_SUCCESS : MKPP_ERROR_DEVICE;
 }
 

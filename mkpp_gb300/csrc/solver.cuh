@@ -61,11 +61,12 @@ struct LaunchArgs {
   // starts from the previous call's carry, and the last call's carry is
   // written back (Controller::carry_out).
   double* dt_carry;
-  // Split launch: the first split_cells entries of order are integrated by
-  // whole warps (integrate_split_kernel, launched beside the persistent
-  // kernel), which takes its cells from order[split_cells..]; split_next is
+  // Split launch (integrate_split_kernel): the first split_cells entries of
+  // order are integrated by whole warps on the SMs with id < split_sms, the
+  // persistent body takes its cells from order[split_cells..]; split_next is
   // the warps' work counter (zeroed before launch).
   int split_cells;
+  int split_sms;
   unsigned int* split_next;
 };
 
@@ -154,11 +155,11 @@ struct StoreFor {
 };
 
 template <class Mech>
-__device__ __forceinline__ TileStore make_store(double* scratch, TileStore*) {
-  return TileStore{scratch + (size_t)blockIdx.x * Mech::NSLOTS * kBlock + threadIdx.x};
+__device__ __forceinline__ TileStore make_store(double* scratch, TileStore*, unsigned block = blockIdx.x) {
+  return TileStore{scratch + (size_t)block * Mech::NSLOTS * kBlock + threadIdx.x};
 }
 template <class Mech, int N>
-__device__ __forceinline__ RegStore<N> make_store(double*, RegStore<N>*) {
+__device__ __forceinline__ RegStore<N> make_store(double*, RegStore<N>*, unsigned = 0) {
   return RegStore<N>{};
 }
 
@@ -338,10 +339,12 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_plain_kernel(LaunchArg
 // so a warp's lanes stay busy even when cells need very different numbers
 // of attempts.  All lanes run the same attempt code on different cells.
 // ---------------------------------------------------------------------------
-template <class Mech, int MINB, bool TAIL = false>
-__global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
+// The persistent kernel's body for one block (its tile is scratch tile
+// `block`); integrate_split_kernel runs it on the SMs it does not reserve.
+template <class Mech, bool TAIL>
+__device__ __forceinline__ void persistent_body(const LaunchArgs& a, double* scratch, unsigned block) {
   using Store = typename StoreFor<Mech>::type;
-  Store S = make_store<Mech>(scratch, (Store*)nullptr);
+  Store S = make_store<Mech>(scratch, (Store*)nullptr, block);
   const size_t n = (size_t)a.ncells;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -451,6 +454,12 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(Laun
   }
 }
 
+template <class Mech, int MINB, bool TAIL = false>
+__global__ void __launch_bounds__(kBlock, MINB) integrate_persistent_kernel(LaunchArgs a, double* scratch) {
+  persistent_body<Mech, TAIL>(a, scratch, blockIdx.x);
+}
+
+
 // ---------------------------------------------------------------------------
 // Cooperative form for parked cells: a whole warp integrates one cell at a
 // time, the cell's working set in shared memory, each attempt spread over
@@ -538,17 +547,27 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
 }
 
 // ---------------------------------------------------------------------------
-// Split form: launched beside the persistent kernel (on another stream, on
-// SM resources the persistent grid leaves free), whole warps integrate the
-// first split_cells cells of the order, the most expensive ones, from their
-// start.  A warp finishes a SAPRC99 attempt in ~0.37 ms against ~1.3 ms on
-// one lane, so the cells that would set the makespan on lanes finish sooner.
-// Each warp takes the next cell from a.split_next.  Results are
-// bit-identical to the other forms (attempt_coop reproduces attempt).
+// Split form: one launch in which the blocks on the first split_sms SMs
+// (by the SM id the hardware reports) integrate the first split_cells cells
+// of the order, the most expensive ones, each on a whole warp from its
+// start, while the blocks on the other SMs run the persistent body over the
+// rest of the order.  A warp finishes a SAPRC99 attempt ~3x sooner than a
+// lane when its SM runs no lanes, so the cells that would set the end of
+// the launch on lanes finish earlier; reserving whole SMs keeps the
+// persistent blocks' FP64 work off those warps' SMs.  Each warp takes the
+// next cell from a.split_next.  Results are bit-identical to the other
+// forms (attempt_coop reproduces attempt).  Every block has the
+// warp-cooperative stores as dynamic shared memory.
 // ---------------------------------------------------------------------------
 template <class Mech>
-__global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_split_kernel(LaunchArgs a) {
+__global__ void __launch_bounds__(kBlock, 2) integrate_split_kernel(LaunchArgs a, double* scratch) {
   extern __shared__ double smem[];
+  unsigned smid;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  if (smid >= (unsigned)a.split_sms) {
+    persistent_body<Mech, false>(a, scratch, blockIdx.x);
+    return;
+  }
   const unsigned lane = threadIdx.x & 31u;
   double* S = smem + (size_t)(threadIdx.x >> 5) * Mech::COOP_SLOTS;
   const size_t n = (size_t)a.ncells;

@@ -90,11 +90,11 @@ def test_tail_parking_leaves_results_unchanged(built_libs, mech):
 
 @pytest.mark.parametrize("mech", ["small_strato", "saprc99"])
 def test_split_launch_leaves_results_unchanged(built_libs, mech):
-    """mkpp_set_split_launch: the first cells of the order on whole warps
-    beside the persistent kernel (a window of 2 host steps, 640 cells, the
-    order reversed, its first 40 cells on 4 blocks).  State, status, attempt
-    counts and carried step sizes end bit-identical to the launch without
-    the split, with and without step-size carry-over."""
+    """mkpp_set_split_launch: the first cells of the order on whole warps of
+    reserved SMs, the rest on the persistent body (a window of 2 host steps,
+    640 cells, the order reversed, its first 40 cells on 4 SMs).  State,
+    status, attempt counts and carried step sizes end bit-identical to the
+    launch without the split, with and without step-size carry-over."""
     import torch
 
     from mkpp_gb300.api import DeviceSolver
