@@ -107,6 +107,9 @@ def parse():
     ap.add_argument("--bulk-defer", type=int, default=0,
                     help="park each cell for the warp-cooperative kernel after this many attempts (0: never); "
                          "1 with few cells measures the cooperative kernel's attempt latency")
+    ap.add_argument("--tune", type=int, default=1,
+                    help="1: the warm-up windows compare launch configurations (default, tail parking, split "
+                         "launch) and the fastest is timed; 0: time the flags' configuration")
     ap.add_argument("--split", default="auto",
                     help="split launch of the window (mkpp_set_split_launch): 'auto' plans it from the first "
                          "warm-up window's attempt counts and keeps it only if a warm-up window with it beats one "
@@ -375,13 +378,36 @@ def cpu_integrate(runner, sub, conc, first: int, last: int, threads: int, chunk:
     return time.perf_counter() - t0
 
 
-def cpu_reference_sample(w, cells: int, host_steps: int, threads: int, chunk: int = 64):
+def cpu_reference_sample(w, cells: int, host_steps: int, threads: int, chunk: int = 64, out=None):
     """Time the CPU implementation on the first `cells` cells of the workload,
-    all host steps."""
+    all host steps (the end state goes to `out` when given)."""
     sub = w.subset(cells)
     kind, runner = cpu_runner(sub.mechanism)
-    el = cpu_integrate(runner, sub, sub.conc.copy(), 0, host_steps, threads, chunk)
+    conc = sub.conc.copy()
+    el = cpu_integrate(runner, sub, conc, 0, host_steps, threads, chunk)
+    if out is not None:
+        out.append(conc)
     return kind, cells * host_steps / el, el
+
+
+def parity_against(got, ref, raw) -> dict:
+    """The GPU window's end state against the CPU solver's on the same cells:
+    per species |got - ref| in units of rtol |ref| + atol (the tolerance),
+    and relative to |ref| + atol."""
+    atol = np.array(raw["atol"])[:, None]
+    rtol = np.array(raw["rtol"])[:, None]
+    both = np.isfinite(got).all(axis=0) & np.isfinite(ref).all(axis=0)
+    d = np.abs(got - ref)[:, both]
+    r = np.abs(ref)[:, both]
+    tol_units = d / (rtol * r + atol)
+    per_cell = tol_units.max(axis=0) if both.any() else np.zeros(0)
+    return {"cells": int(got.shape[1]), "both_finite": int(both.sum()),
+            "nonfinite_same_cells": bool(np.array_equal(~np.isfinite(got).all(axis=0),
+                                                        ~np.isfinite(ref).all(axis=0))),
+            "max_error_tolerance_units": float(tol_units.max()) if both.any() else None,
+            "median_relative_error": float(np.median(d / (r + atol))) if both.any() else None,
+            "cells_within_tolerance_frac": float((per_cell <= 1.0).mean()) if both.any() else None,
+            "cells_within_10x_tolerance_frac": float((per_cell <= 10.0).mean()) if both.any() else None}
 
 
 def run_reference(args, world, rank):
@@ -522,16 +548,21 @@ def main():
         if args.order:
             order.copy_(torch.argsort(acc + rej, descending=True).to(torch.int32))
 
-    # Split launch: planned from the first warm-up window's attempt counts
-    # with the per-attempt times of a lane (all lanes busy) and of a whole
-    # warp, both measured here on capped cells; kept only if a warm-up
-    # window with it beats one without (same cost order).
-    split = (0, 0)
-    split_info = {"mode": args.split}
-    if args.split not in ("auto", "off"):
-        split = tuple(int(x) for x in args.split.split(":"))
-    t_lane = t_warp = None
-    if args.split == "auto" and args.order and args.warmup >= 2:
+    # Launch tuning in the warm-up windows.  Window 0 runs in cell order and
+    # gives every cell's attempt count; each later warm-up window (now in
+    # cost order) runs one candidate launch configuration, and the fastest
+    # is the one timed:
+    #   default   the library's settings;
+    #   tail      tail parking after 300 attempts (mkpp_set_tail_parking);
+    #   split     the split launch (mkpp_set_split_launch), planned from the
+    #             window-0 attempt counts with the per-attempt times of a
+    #             lane (all lanes busy) and of a whole warp, measured here.
+    # Every candidate gives bit-identical results.  --tune 0 times the
+    # configuration the flags give, unchanged.
+    tune_info = {"tuned": bool(args.tune and args.order and args.warmup >= 2)}
+    fixed_split = (0, 0) if args.split in ("auto", "off") else tuple(int(x) for x in args.split.split(":"))
+    t_warp = None
+    if tune_info["tuned"] and args.split == "auto":
         defer_default = int(os.environ.get("MKPP_DEFER_AFTER", "3000"))
         blocks_env = int(os.environ.get("MKPP_BLOCKS_PER_SM", "0"))
         b_lane = bulk_rate(w.mechanism, min(n, 77824), 20, stream)
@@ -539,53 +570,59 @@ def main():
         solver.set_tuning(0, blocks_env, defer_default)
         # 39 of the 40 attempts run on a warp; x1.2 for 8 warps on an SM
         t_warp = 1.2 * b_warp["ms"] * 1e-3 / 39.0
-        split_info.update(t_warp_s=t_warp, bulk_attempts_per_s=b_lane["attempts_per_s"])
+        tune_info.update(t_warp_s=t_warp, bulk_attempts_per_s=b_lane["attempts_per_s"])
 
-    # Warm-up windows, eager, with events around the integrate launch.
+    def apply_config(cfg):
+        solver.set_tail_parking(cfg["tail"])
+        solver.set_split_launch(*cfg["split"])
+
+    configs = [{"name": "default", "tail": args.tail_after, "split": (0, 0) if tune_info["tuned"] else fixed_split}]
+    if tune_info["tuned"]:
+        if args.tail_after == 0:
+            configs.append({"name": "tail", "tail": 300, "split": (0, 0)})
+        if args.split != "off":
+            configs.append({"name": "split", "tail": 0, "split": fixed_split})
     ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     kernel_ms = []
-    timed_cfg_ms = []      # warm-up windows run with the configuration that is timed
+    cfg_of = []            # the configuration each warm-up window ran
+    chosen = configs[0]
+    apply_config(chosen)
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
-            if args.split == "auto" and t_warp is not None:
-                if i == 1:
+            if tune_info["tuned"] and i >= 1:
+                if i == 1 and t_warp is not None:
                     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-                    # resident blocks of 128 lanes: 2 per SM for the 255-register
-                    # variant, 4 for the 128-register one (or the cap set)
                     per_sm = 4 if os.environ.get("MKPP_REGISTER_VARIANT") == "4" else 2
                     if int(os.environ.get("MKPP_BLOCKS_PER_SM", "0")) > 0:
                         per_sm = min(per_sm, int(os.environ["MKPP_BLOCKS_PER_SM"]))
-                    t_lane = per_sm * sms * 128 / split_info["bulk_attempts_per_s"]
+                    t_lane = per_sm * sms * 128 / tune_info["bulk_attempts_per_s"]
                     k, b, span = split_plan((acc + rej).cpu().numpy(), sms, t_lane, t_warp, per_sm)
-                    split = (k, b)
-                    split_info.update(sms=sms, t_lane_s=t_lane, planned_cells_sms=[k, b],
-                                      modelled_ms=span * 1e3)
-                    solver.set_split_launch(*split)
-                elif i == 2:
-                    solver.set_split_launch(0, 0)
-                elif i == 3:
-                    use = split != (0, 0) and kernel_ms[1] < kernel_ms[2]
-                    split_info["kept"] = bool(use)
-                    if not use:
-                        split = (0, 0)
-                    solver.set_split_launch(*split)
-                    timed_cfg_ms = [kernel_ms[1] if use else kernel_ms[2]]
-            elif i == 0 and split != (0, 0):
-                solver.set_split_launch(*split)
+                    tune_info.update(t_lane_s=t_lane, split_plan_cells_sms=[k, b], split_modelled_ms=span * 1e3)
+                    for c in configs:
+                        if c["name"] == "split":
+                            c["split"] = (k, b)
+                    configs = [c for c in configs if c["name"] != "split" or c["split"] != (0, 0)]
+                pending = [c for c in configs if "ms" not in c]
+                if pending:
+                    chosen = pending[0]
+                else:
+                    chosen = min(configs, key=lambda c: c["ms"])
+                apply_config(chosen)
             window(ev)
             stream.synchronize()
             kernel_ms.append(ev[0].elapsed_time(ev[1]))
-            if i >= 3 or (args.split != "auto" and i >= 1):
-                timed_cfg_ms.append(kernel_ms[-1])
-            log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms (split {split})")
-        if args.split == "auto" and t_warp is not None and args.warmup == 3:
-            use = split != (0, 0) and kernel_ms[1] < kernel_ms[2]
-            split_info["kept"] = bool(use)
-            if not use:
-                split = (0, 0)
-            solver.set_split_launch(*split)
-            timed_cfg_ms = [kernel_ms[1] if use else kernel_ms[2]]
-    split_info["cells_sms"] = list(split)
+            cfg_of.append(chosen["name"])
+            if i >= 1 and "ms" not in chosen:
+                chosen["ms"] = kernel_ms[-1]
+            log(f"warm-up window {i}: integrate {kernel_ms[-1]:.0f} ms ({chosen['name']})")
+        if tune_info["tuned"]:
+            measured = [c for c in configs if "ms" in c]
+            chosen = min(measured, key=lambda c: c["ms"]) if measured else configs[0]
+            apply_config(chosen)
+    tune_info["candidates_ms"] = {c["name"]: c.get("ms") for c in configs}
+    tune_info["chosen"] = {"name": chosen["name"], "tail_after": chosen["tail"], "split_cells_sms": list(chosen["split"])}
+    split = tuple(chosen["split"])
+    timed_cfg_ms = [ms for i, (ms, name) in enumerate(zip(kernel_ms, cfg_of)) if i >= 1 and name == chosen["name"]]
     if not timed_cfg_ms:
         timed_cfg_ms = kernel_ms[1:] or kernel_ms
     # Capture the window: hs rate-constant launches, the persistent integrate
@@ -608,7 +645,12 @@ def main():
     barrier(world)
     el_ms = max_over_ranks(start.elapsed_time(end), world) / args.steps
     log(f"timed: {el_ms:.0f} ms per window")
-    solver.set_split_launch(0, 0)   # the later sections run without it
+    # End state of the timed window's first cells, for the parity check
+    # against the CPU reference solver on the same cells (cpu_baseline).
+    window_end = conc[:, :min(n, cpu_sample_cells(args, os.cpu_count() or 1))].cpu().numpy()
+    # The later sections run with the library's defaults and the flags.
+    solver.set_split_launch(0, 0)
+    solver.set_tail_parking(args.tail_after)
     clk = clocks.summary()
     cell_solves = shard.sum_over_ranks(n * hs)
     value = cell_solves / (el_ms * 1e-3)
@@ -645,12 +687,12 @@ def main():
         "warmup": args.warmup, "ms_per_step": el_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(w, hs),
         "gpu_launches": args.steps * (hs + 1 + (int(os.environ.get("MKPP_DEFER_AFTER", "3000")) > 0
-                                                or args.tail_after > 0) + (split != (0, 0))),
+                                                or chosen["tail"] > 0)),
         "launch": {"register_variant": os.environ.get("MKPP_REGISTER_VARIANT", "2"),
                    "blocks_per_sm": os.environ.get("MKPP_BLOCKS_PER_SM", "max"),
                    "defer_after_per_host_step": os.environ.get("MKPP_DEFER_AFTER", "3000"), "cost_order": bool(args.order),
-                   "tail_after": args.tail_after,
-                   "max_attempts_per_call": args.max_attempts, "split": split_info},
+                   "tail_after": chosen["tail"],
+                   "max_attempts_per_call": args.max_attempts, "tuning": tune_info},
         "clocks": clk,
         "work": {"attempts_per_cell_solve": attempts / (n * hs), "flops_per_attempt": fpa["total"],
                  "attempts_per_cell_window_pct": {q: float(np.percentile(att, q)) for q in (50, 90, 99, 100)},
@@ -829,7 +871,8 @@ def main():
         with optional_section(result, "cpu_baseline", True):
             threads = os.cpu_count() or 1
             cells = min(cpu_sample_cells(args, threads), n)
-            kind, v, el = cpu_reference_sample(w, cells, hs, threads, args.cpu_chunk)
+            cpu_end = []
+            kind, v, el = cpu_reference_sample(w, cells, hs, threads, args.cpu_chunk, cpu_end)
             log(f"cpu baseline ({kind}): {el:.1f} s")
             # The sample's cost mix against the whole run's, from the GPU's
             # attempt counters on the same cells (the CPU solver runs the
@@ -841,7 +884,10 @@ def main():
                           f"OMP_PLACES={os.environ.get('OMP_PLACES')}",
                 "seconds": el,
                 "attempts_per_cell_solve_sample": float(att[:cells].sum()) / (cells * hs),
-                "attempts_per_cell_solve_run": attempts / (n * hs)}
+                "attempts_per_cell_solve_run": attempts / (n * hs),
+                # the timed window's end state on these cells against the CPU
+                # solver's, all host steps
+                "parity": parity_against(window_end[:, :cells], cpu_end[0], raw)}
 
     if rank == 0 and world == 1:
         with optional_section(result, "bulk", True):

@@ -70,8 +70,7 @@ int set_coop_smem(size_t bytes);
 int launch_coop(const mkpp::LaunchArgs& a, int grid, int threads, size_t smem, cudaStream_t stream);
 // ... and the split form (integrate_split_kernel: whole warps on reserved
 // SMs, the persistent body on the others).
-int set_split_smem(size_t bytes);
-int launch_split(const mkpp::LaunchArgs& a, double* scratch, int grid, size_t smem, cudaStream_t stream);
+int launch_split(const mkpp::LaunchArgs& a, double* scratch, int grid, cudaStream_t stream);
 // mkpp_checkpoint.cu, mkpp_replay.cu, mkpp_adjoint.cu: differentiation kernels.
 int launch_checkpoint(const mkpp::LaunchArgs& a, const mkpp::CheckpointArgs& ck, double* scratch, int grid,
                       cudaStream_t stream);

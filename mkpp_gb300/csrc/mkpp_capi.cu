@@ -187,7 +187,7 @@ const LaunchConfig& launch_config() {
     cfg.coop_warps = (int)std::min<size_t>(mkpp::kCoopWarps, (200u * 1024u) / per_warp);
     cfg.coop_smem = per_warp * (size_t)std::max(1, cfg.coop_warps);
     cfg.coop_ok = cfg.coop_warps >= 1 && set_coop_smem(cfg.coop_smem) == MKPP_SUCCESS;
-    cfg.split_ok = cfg.coop_ok && set_split_smem(cfg.coop_smem) == MKPP_SUCCESS;
+    cfg.split_ok = StoreInfo::kTile;
   }
   return cfg;
 }
@@ -235,7 +235,7 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
     // in the same launch as the persistent body (255-register variant, a
     // whole warp's store fitting the block's shared memory).
     const bool split = t.split_cells > 0 && t.split_sms > 0 && t.split_sms < cfg.sms && a.order && cfg.split_ok &&
-                       cfg.minb == 2 && t.tail_after == 0 && cfg.coop_warps * 32 == mkpp::kBlock;
+                       cfg.minb == 2 && t.tail_after == 0;
     if (split) {
       a.split_cells = (int)std::min<long long>(t.split_cells, a.ncells);
       a.split_sms = t.split_sms;
@@ -252,7 +252,7 @@ int launch_integrate(const mkpp::LaunchArgs& args, int mode, void* workspace, cu
       a.tail_cells = (unsigned)(cfg.sms * 2 * cfg.coop_warps);
       if (launch_persistent_tail(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else if (split) {
-      if (launch_split(a, scratch, cfg.grid, cfg.coop_smem, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
+      if (launch_split(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else if (cfg.minb == 4) {
       if (launch_persistent4(a, scratch, cfg.grid, stream) != MKPP_SUCCESS) return MKPP_ERROR_DEVICE;
     } else {

@@ -556,12 +556,15 @@ __global__ void __launch_bounds__(kCoopWarps * 32, 1) integrate_coop_kernel(Laun
 // the launch on lanes finish earlier; reserving whole SMs keeps the
 // persistent blocks' FP64 work off those warps' SMs.  Each warp takes the
 // next cell from a.split_next.  Results are bit-identical to the other
-// forms (attempt_coop reproduces attempt).  Every block has the
-// warp-cooperative stores as dynamic shared memory.
+// forms (attempt_coop reproduces attempt).  A warp's store is a slice of its
+// block's scratch tile (unused by the persistent body there), so the launch
+// needs no shared memory and the persistent blocks keep the whole L1.
 // ---------------------------------------------------------------------------
 template <class Mech>
 __global__ void __launch_bounds__(kBlock, 2) integrate_split_kernel(LaunchArgs a, double* scratch) {
-  extern __shared__ double smem[];
+  static_assert(kCoopWarps * 32 == kBlock, "a split block is kCoopWarps warps");
+  static_assert((size_t)kCoopWarps * Mech::COOP_SLOTS <= StoreFor<Mech>::block_bytes / sizeof(double),
+                "the warps' stores fit in the block's scratch tile");
   unsigned smid;
   asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
   if (smid >= (unsigned)a.split_sms) {
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(kBlock, 2) integrate_split_kernel(LaunchArgs a
     return;
   }
   const unsigned lane = threadIdx.x & 31u;
-  double* S = smem + (size_t)(threadIdx.x >> 5) * Mech::COOP_SLOTS;
+  double* S = scratch + (size_t)blockIdx.x * Mech::NSLOTS * kBlock + (size_t)(threadIdx.x >> 5) * Mech::COOP_SLOTS;
   const size_t n = (size_t)a.ncells;
   // Every pass takes a new counter value, so a warp makes at most
   // split_cells + 1 passes.
