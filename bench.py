@@ -97,9 +97,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--tangent", type=int, default=0,
                     help="also time the tangent sweep over the adjoint section's checkpoints (mkpp_gpu_tangent)")
-    ap.add_argument("--tail-after", type=int, default=0,
+    ap.add_argument("--tail-after", type=int, default=None,
                     help="tail parking threshold in attempts for every integrate launch (mkpp_set_tail_parking; 0 off)")
-    ap.add_argument("--e2e-cost-order", type=int, default=0,
+    ap.add_argument("--e2e-cost-order", type=int, default=1,
                     help="e2e handle hands out the previous call's most expensive cells first (mkpp_set_cost_order)")
     ap.add_argument("--bulk-cells", type=int, default=77824,
                     help="cells of the bulk-rate section (every cell capped at --bulk-attempts attempts)")
@@ -311,36 +311,6 @@ def adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, window_ms) ->
     return out
 
 
-def split_plan(att, sms: int, t_lane: float, t_warp: float, blocks_per_sm: int = 2, warps_per_block: int = 4):
-    """(cells, reserved SMs, modelled seconds) of the split launch for a
-    window whose cells need `att` attempts each (the previous window's
-    counts).  Cells are handed out most expensive first.  Model: the first
-    `cells` cells run on the whole warps of the reserved SMs at t_warp
-    seconds per attempt, the rest on the lanes of the other SMs at t_lane
-    seconds per attempt per lane (all lanes busy); each side ends when its
-    total work is done or its largest cell is, whichever is later.  (0, 0, t)
-    is the launch without the split."""
-    c = np.sort(np.asarray(att, dtype=np.float64))[::-1]
-    pre = np.concatenate([[0.0], np.cumsum(c)])
-    total = pre[-1]
-    lanes_per_sm = blocks_per_sm * 128
-    best = (0, 0, max(total * t_lane / (sms * lanes_per_sm), c[0] * t_lane))
-    ks = np.unique(np.concatenate([np.arange(0, min(len(c), 256)), np.geomspace(256, len(c), 64).astype(int)]))
-    ks = ks[(ks > 0) & (ks < len(c))]
-    for reserved in (1, 2, 4, 6, 8, 12, 16, 24, 32):
-        if reserved >= sms:
-            break
-        warps = reserved * blocks_per_sm * warps_per_block
-        lanes = (sms - reserved) * lanes_per_sm
-        coop = np.maximum(pre[ks] * t_warp / warps, c[0] * t_warp)
-        lane = np.maximum((total - pre[ks]) * t_lane / lanes, c[ks] * t_lane)
-        span = np.maximum(coop, lane)
-        j = int(np.argmin(span))
-        if span[j] < best[2]:
-            best = (int(ks[j]), reserved, float(span[j]))
-    return best
-
-
 def cpu_sample_cells(args, threads: int) -> int:
     """Cells of the CPU sample: at least 4096, and at least one 64-cell chunk
     of the reference's static OpenMP schedule per thread."""
@@ -499,8 +469,10 @@ def main():
     plan = load(w.mechanism)
     lib = load_library(w.mechanism)
     solver = DeviceSolver(w.mechanism)
-    if args.tail_after:
-        solver.set_tail_parking(args.tail_after)
+    # Tail parking threshold the runs use unless the tuning below picks
+    # another: the flag, else the library's default (MKPP_TAIL_AFTER or 300).
+    lib_tail = args.tail_after if args.tail_after is not None else int(os.environ.get("MKPP_TAIL_AFTER", "300"))
+    solver.set_tail_parking(lib_tail)
     NS, NR, NP = solver.sizes.species, solver.sizes.reactions, solver.sizes.rate_parameters
     seed = float(raw["initial_step_seed"])
 
@@ -552,36 +524,35 @@ def main():
     # gives every cell's attempt count; each later warm-up window (now in
     # cost order) runs one candidate launch configuration, and the fastest
     # is the one timed:
-    #   default   the library's settings;
-    #   tail      tail parking after 300 attempts (mkpp_set_tail_parking);
-    #   split     the split launch (mkpp_set_split_launch), planned from the
-    #             window-0 attempt counts with the per-attempt times of a
-    #             lane (all lanes busy) and of a whole warp, measured here.
+    #   default   the library's settings (tail parking after 300 attempts);
+    #   tail      tail parking after 300 attempts, where the flags turned it
+    #             off (mkpp_set_tail_parking);
+    #   split     the split launch (mkpp_set_split_launch): the 0.1% most
+    #             expensive cells of the previous window on whole warps of
+    #             one reserved SM per 25 of them (SAPRC99, 262144 cells: 262
+    #             cells on 10 SMs; measured there, 200 cells on 8 SMs took
+    #             the window from 38.3 s to 32.3 s, and a model-planned 23
+    #             cells on 1 SM lengthened it to 41.3 s).
     # Every candidate gives bit-identical results.  --tune 0 times the
     # configuration the flags give, unchanged.
     tune_info = {"tuned": bool(args.tune and args.order and args.warmup >= 2)}
     fixed_split = (0, 0) if args.split in ("auto", "off") else tuple(int(x) for x in args.split.split(":"))
-    t_warp = None
-    if tune_info["tuned"] and args.split == "auto":
-        defer_default = int(os.environ.get("MKPP_DEFER_AFTER", "3000"))
-        blocks_env = int(os.environ.get("MKPP_BLOCKS_PER_SM", "0"))
-        b_lane = bulk_rate(w.mechanism, min(n, 77824), 20, stream)
-        b_warp = bulk_rate(w.mechanism, 152, 40, stream, defer=1)
-        solver.set_tuning(0, blocks_env, defer_default)
-        # 39 of the 40 attempts run on a warp; x1.2 for 8 warps on an SM
-        t_warp = 1.2 * b_warp["ms"] * 1e-3 / 39.0
-        tune_info.update(t_warp_s=t_warp, bulk_attempts_per_s=b_lane["attempts_per_s"])
+    if args.split == "auto":
+        k = max(1, round(n * 1e-3))
+        auto_split = (k, max(1, min(16, round(k / 25))))
+    else:
+        auto_split = fixed_split
 
     def apply_config(cfg):
         solver.set_tail_parking(cfg["tail"])
         solver.set_split_launch(*cfg["split"])
 
-    configs = [{"name": "default", "tail": args.tail_after, "split": (0, 0) if tune_info["tuned"] else fixed_split}]
+    configs = [{"name": "default", "tail": lib_tail, "split": (0, 0) if tune_info["tuned"] else fixed_split}]
     if tune_info["tuned"]:
-        if args.tail_after == 0:
+        if lib_tail == 0:
             configs.append({"name": "tail", "tail": 300, "split": (0, 0)})
         if args.split != "off":
-            configs.append({"name": "split", "tail": 0, "split": fixed_split})
+            configs.append({"name": "split", "tail": 0, "split": auto_split})
     ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     kernel_ms = []
     cfg_of = []            # the configuration each warm-up window ran
@@ -590,19 +561,10 @@ def main():
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
             if tune_info["tuned"] and i >= 1:
-                if i == 1 and t_warp is not None:
-                    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-                    per_sm = 4 if os.environ.get("MKPP_REGISTER_VARIANT") == "4" else 2
-                    if int(os.environ.get("MKPP_BLOCKS_PER_SM", "0")) > 0:
-                        per_sm = min(per_sm, int(os.environ["MKPP_BLOCKS_PER_SM"]))
-                    t_lane = per_sm * sms * 128 / tune_info["bulk_attempts_per_s"]
-                    k, b, span = split_plan((acc + rej).cpu().numpy(), sms, t_lane, t_warp, per_sm)
-                    tune_info.update(t_lane_s=t_lane, split_plan_cells_sms=[k, b], split_modelled_ms=span * 1e3)
-                    for c in configs:
-                        if c["name"] == "split":
-                            c["split"] = (k, b)
-                    configs = [c for c in configs if c["name"] != "split" or c["split"] != (0, 0)]
-                pending = [c for c in configs if "ms" not in c]
+                # the likely winners first: with the default three warm-up
+                # windows only two candidates get a window
+                rank = {"split": 0, "tail": 1, "default": 2}
+                pending = sorted((c for c in configs if "ms" not in c), key=lambda c: rank[c["name"]])
                 if pending:
                     chosen = pending[0]
                 else:
@@ -650,7 +612,7 @@ def main():
     window_end = conc[:, :min(n, cpu_sample_cells(args, os.cpu_count() or 1))].cpu().numpy()
     # The later sections run with the library's defaults and the flags.
     solver.set_split_launch(0, 0)
-    solver.set_tail_parking(args.tail_after)
+    solver.set_tail_parking(lib_tail)
     clk = clocks.summary()
     cell_solves = shard.sum_over_ranks(n * hs)
     value = cell_solves / (el_ms * 1e-3)
@@ -842,8 +804,7 @@ def main():
             conc_np, par_np = work_conc.numpy(), [x.numpy() for x in host_par]
             ctx.set_state(conc_np, t_h.numpy(), p_h.numpy(), r_h.numpy())
             ctx.set_aerosol(relative_humidity=rh_h.numpy())
-            if args.e2e_cost_order:
-                ctx.set_cost_order(True)
+            ctx.set_cost_order(bool(args.e2e_cost_order))
             e2e_times = []
             for rep in range(1):
                 work_conc.copy_(host_conc)

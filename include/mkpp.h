@@ -100,11 +100,12 @@ int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts);
 /* Read back the per-cell status / accepted / rejected counts of the last
  * mkpp_integrate (each array num_cells ints; any may be NULL). */
 int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* rejected);
-/* Cost ordering (default off): each mkpp_integrate hands out first the cells
+/* Cost ordering (default on): each mkpp_integrate hands out first the cells
  * that needed the most attempts in the previous call on this handle, so the
  * slowest cells start first and the call's tail shrinks.  Results do not
  * depend on it (cells are independent); it reads back num_cells x 2 ints per
- * call.  enable 0 turns it off and forgets the counts. */
+ * call and sends the order (num_cells ints).  enable 0 turns it off and
+ * forgets the counts. */
 int mkpp_set_cost_order(mkpp_handle_t handle, int enable);
 /* Step-size carry-over (default off; no reference entry: the reference
  * restarts every integrate() at dt * initial_step_seed and lists carried
@@ -148,8 +149,8 @@ size_t mkpp_gpu_workspace_bytes(size_t num_cells);
  * Results do not depend on it: a handed-off cell ends bit-identical. */
 int mkpp_set_launch_tuning(int register_variant, int blocks_per_sm, int defer_after);
 
-/* Process-wide tail parking of the persistent integrate kernel (default 0:
- * off; environment MKPP_TAIL_AFTER).  Once every cell of a launch has been
+/* Process-wide tail parking of the persistent integrate kernel (default 300
+ * attempts, 0: off; environment MKPP_TAIL_AFTER).  Once every cell of a launch has been
  * handed out and no more cells are still on lanes than the warp-cooperative
  * kernel runs at once, a cell with at least min_attempts attempts is parked
  * for that kernel, which takes a warp per cell.  The last, slowest cells of a

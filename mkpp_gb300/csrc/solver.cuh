@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(kBlock, 2) integrate_split_kernel(LaunchArgs a
   static_assert((size_t)kCoopWarps * Mech::COOP_SLOTS <= StoreFor<Mech>::block_bytes / sizeof(double),
                 "the warps' stores fit in the block's scratch tile");
   unsigned smid;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  asm("mov.u32 %0, %%smid;" : "=r"(smid));  // the SM this block runs on
   if (smid >= (unsigned)a.split_sms) {
     persistent_body<Mech, false>(a, scratch, blockIdx.x);
     return;
