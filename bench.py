@@ -563,8 +563,8 @@ def main():
             if tune_info["tuned"] and i >= 1:
                 # the likely winners first: with the default three warm-up
                 # windows only two candidates get a window
-                rank = {"split": 0, "tail": 1, "default": 2}
-                pending = sorted((c for c in configs if "ms" not in c), key=lambda c: rank[c["name"]])
+                priority = {"split": 0, "tail": 1, "default": 2}
+                pending = sorted((c for c in configs if "ms" not in c), key=lambda c: priority[c["name"]])
                 if pending:
                     chosen = pending[0]
                 else:
