@@ -292,9 +292,6 @@ constexpr int kNoAllocMaxCells = MKPP_NOALLOC_MAX_CELLS;
 // The plain launch gives every block kBlock cells of scratch, so the array
 // covers the last block only when the capacity is a whole number of blocks.
 static_assert(kNoAllocMaxCells % mkpp::kBlock == 0, "noalloc capacity must be a multiple of the block size");
-// The plain launch gives every block kBlock cells of scratch, so the array
-// covers the last block only when the capacity is a whole number of blocks.
-static_assert(kNoAllocMaxCells % mkpp::kBlock == 0, "noalloc capacity must be a multiple of the block size");
 constexpr size_t kNoAllocDoubles = StoreInfo::kTile ? (size_t)kNoAllocMaxCells * Mech::NSLOTS : 1;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 

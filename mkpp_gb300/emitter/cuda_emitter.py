@@ -1211,6 +1211,7 @@ def emit_mechanism(plan: ReducedPlan, table: bool | None = None) -> str:
         c(f"  static constexpr int NSLOTS = {coop['total']};")
     else:
         c(f"  static constexpr int NSLOTS = {nslots};")
+    plan._nslots = coop["total"] if table else nslots
     c(f"  static constexpr bool TABLE_ATTEMPT = {'true' if table else 'false'};")
     c("")
     # With the store in the global tile, fun, jac_w, factor and solve are
@@ -1488,6 +1489,12 @@ def emit_host_header(plan) -> str:
     generated header (src/mkpp/templates/host_api/mkpp.h.j2:29-33)."""
     raw = plan.raw
     guard = f"MKPP_GB300_{plan.name.upper()}_MKPP_H"
+    if not hasattr(plan, "_nslots"):
+        emit_mechanism(plan)
+    # The allocation-free entry's static scratch: NSLOTS doubles for each of
+    # MKPP_NOALLOC_MAX_CELLS cells when the store is the global tile (more
+    # than REGISTER_SLOTS slots), one double when it lives in registers.
+    noalloc = (f"(MKPP_NOALLOC_MAX_CELLS * {plan._nslots} * 8)" if plan._nslots > REGISTER_SLOTS else "8")
     return f"""/*
  * mkpp.h of the {plan.name} library (libmkpp_{plan.name}.so), generated from its plan.
  * The C ABI of include/mkpp.h plus the mechanism's sizes, as the header the
@@ -1504,6 +1511,10 @@ def emit_host_header(plan) -> str:
 #define MKPP_NUM_SPECIES   {len(raw["species"])}
 #define MKPP_NUM_REACTIONS {raw["num_reactions"]}
 #define MKPP_NUM_PHOTOLYSIS {raw["num_photolysis"]}
+
+/* Bytes of device memory that mkpp_gpu_integrate_noalloc's static scratch
+ * holds on every GPU that loads this library, until the process exits. */
+#define MKPP_NOALLOC_SCRATCH_BYTES {noalloc}
 
 #endif
 """

@@ -15,4 +15,8 @@
 #define MKPP_NUM_REACTIONS 4
 #define MKPP_NUM_PHOTOLYSIS 2
 
+/* Bytes of device memory that mkpp_gpu_integrate_noalloc's static scratch
+ * holds on every GPU that loads this library, until the process exits. */
+#define MKPP_NOALLOC_SCRATCH_BYTES 8
+
 #endif

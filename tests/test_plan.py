@@ -71,6 +71,28 @@ def test_generated_header_is_current(mech):
     assert kernels.read_text() == cuda_emitter.emit_solver_kernels_header(plan)
 
 
+def test_noalloc_scratch_size_in_generated_header(tmp_path):
+    """MKPP_NOALLOC_SCRATCH_BYTES of each generated host header equals the
+    static array the library defines: MKPP_NOALLOC_MAX_CELLS x NSLOTS
+    doubles for a tile store, one double for a register store."""
+    import re
+    import subprocess
+    src = tmp_path / "size.c"
+    expected = {"saprc99": 1024 * 2226 * 8, "saprcnov": 1024 * 2111 * 8, "ts1": 1024 * 10395 * 8,
+                "saprc99_mini": 1024 * 150 * 8, "chapman": 8, "small_strato": 8}
+    for mech, want in expected.items():
+        nslots = int(re.search(r"static constexpr int NSLOTS = (\d+);",
+                               (cuda_emitter.GEN_DIR / f"{mech}.cuh").read_text()).group(1))
+        store = 1024 * nslots * 8 if nslots > cuda_emitter.REGISTER_SLOTS else 8
+        assert store == want, mech
+        src.write_text('#include <stdio.h>\n#include "mkpp.h"\n'
+                       'int main(void) { printf("%lld\\n", (long long)(MKPP_NOALLOC_SCRATCH_BYTES)); return 0; }\n')
+        exe = tmp_path / f"size_{mech}"
+        subprocess.run(["gcc", "-std=c11", "-I", str(cuda_emitter.GEN_DIR / "host_api" / mech),
+                        str(src), "-o", str(exe)], check=True)
+        assert int(subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout) == want, mech
+
+
 def test_tableaux_match_reference_coefficients():
     """ROS-3 coefficients as in src/mkpp/rosenbrock.py:40-51 and chapman.hpp:190-191."""
     tab = load_raw("chapman")["tableau"]
