@@ -217,6 +217,13 @@ struct Controller {
   }
 };
 
+// A cell skipped because its input is not finite made no attempt in this
+// call: its counts say so, rather than keeping an earlier call's.
+__device__ __forceinline__ void clear_counts(const LaunchArgs& a, size_t c) {
+  if (a.n_accept) a.n_accept[c] = 0;
+  if (a.n_reject) a.n_reject[c] = 0;
+}
+
 template <class Mech, class SA>
 __device__ __forceinline__ void load_state(const double* conc, size_t c, size_t n, SA& S) {
 #pragma unroll
@@ -322,7 +329,10 @@ __global__ void __launch_bounds__(kBlock, MINB) integrate_plain_kernel(LaunchArg
   const size_t n = (size_t)a.ncells;
   const size_t T = (size_t)gridDim.x * kBlock;
   for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
-    if (a.status && a.status[c] != CELL_SUCCESS) continue;
+    if (a.status && a.status[c] != CELL_SUCCESS) {
+      clear_counts(a, c);
+      continue;
+    }
     load_state<Mech>(a.conc, c, n, S);
     int nacc, nrej;
     const int status = integrate_cell<Mech>(S, a, c, nacc, nrej);
@@ -445,9 +455,10 @@ __device__ __forceinline__ void persistent_body(const LaunchArgs& a, double* scr
         store_state<Mech>(a.conc, cc, n, S);
         if (a.dt_carry) a.dt_carry[cc] = ctl.carry_out();
         if (a.status) a.status[cc] = final_status<Mech>(S, capped, zero_pivot);
-        if (a.n_accept) a.n_accept[cc] = nacc;
-        if (a.n_reject) a.n_reject[cc] = nrej;
       }
+      // (a flagged cell's counts are zero: it made no attempt)
+      if (a.n_accept) a.n_accept[cc] = nacc;
+      if (a.n_reject) a.n_reject[cc] = nrej;
       cell = -1;
       left = true;
     }
@@ -584,7 +595,10 @@ __global__ void __launch_bounds__(kBlock, 2) integrate_split_kernel(LaunchArgs a
     const long long cell = a.order[idx];
     if (cell < 0 || cell >= (long long)n) continue;  // an order entry out of range names no cell
     const size_t c = (size_t)cell;
-    if (a.status && a.status[c] != CELL_SUCCESS) continue;
+    if (a.status && a.status[c] != CELL_SUCCESS) {
+      if (lane == 0) clear_counts(a, c);
+      continue;
+    }
     for (int i = lane; i < Mech::NV; i += 32) S[Mech::Y + i] = a.conc[c + n * Mech::var_phys(i)];
     __syncwarp();
     Controller ctl;
@@ -633,7 +647,11 @@ __global__ void __launch_bounds__(kBlock, 2) integrate_checkpoint_kernel(LaunchA
   const size_t n = (size_t)a.ncells;
   const size_t T = (size_t)gridDim.x * kBlock;
   for (size_t c = blockIdx.x * (size_t)kBlock + threadIdx.x; c < n; c += T) {
-    if (a.status && a.status[c] != CELL_SUCCESS) continue;
+    if (a.status && a.status[c] != CELL_SUCCESS) {
+      ck.n[c] = 0;  // no accepted step to revisit
+      clear_counts(a, c);
+      continue;
+    }
     load_state<Mech>(a.conc, c, n, S);
     load_rates<Mech>(a, c, 0, S);
     auto k = [&](int r) { return S[Mech::KT + r]; };

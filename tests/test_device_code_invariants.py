@@ -130,9 +130,9 @@ def test_checkpoint_sweeps_read_clamped_counts():
     """The replay, adjoint and tangent sweeps read a cell's recorded-step
     count through CheckpointArgs::count (clamped to [0, cap]), since the
     device entries take the count array from the caller; only the forward
-    that records the steps writes n[c] itself."""
+    that records the steps writes n[c] itself (0 for a cell it skips)."""
     code = _code(HANDWRITTEN[0])
     reads = re.findall(r"ck\.n\[c\][^\n;]*", code)
-    assert reads == ["ck.n[c] = cnt"]
+    assert reads == ["ck.n[c] = 0", "ck.n[c] = cnt"]
     assert len(re.findall(r"ck\.count\(c\)", code)) == 3
     assert re.search(r"int count\(size_t c\) const \{ return min\(max\(n\[c\], 0\), cap\); \}", code)

@@ -210,6 +210,35 @@ def test_non_finite_cell_is_isolated(built_libs, mode):
     assert np.isnan(conc[0, 5].item())
 
 
+@pytest.mark.parametrize("mech", ["chapman", "saprc99"])
+def test_skipped_cell_reports_no_attempts(built_libs, mech):
+    """mkpp_get_cell_stats describes the last call: a cell whose state turned
+    non-finite between two calls is skipped (status 2) with zero accepted
+    and rejected counts, not the counts of the call before."""
+    from mkpp_gb300.api import MechanismContext
+
+    w = workloads.make(mech, 64)
+    host = np.ascontiguousarray(w.conc.copy())
+    ctx = MechanismContext(mech, 64)
+    try:
+        ctx.set_state(host, w.temp.copy(), w.pressure.copy(), w.rho.copy())
+        ctx.set_aerosol(relative_humidity=w.rh.copy())
+        ctx.set_rate_parameters(np.ascontiguousarray(w.param))
+        ctx.integrate(w.dt)
+        st, acc, rej = ctx.cell_stats()
+        assert st[5] == 0 and acc[5] + rej[5] > 0
+        host[:, 5] = np.nan
+        ctx.integrate(w.dt)
+        st2, acc2, rej2 = ctx.cell_stats()
+    finally:
+        ctx.close()
+    # (in the SAPRC99 sample cell 36 ends non-finite in the first call, so the
+    # second skips it too)
+    skipped = st2 == 2
+    assert skipped[5] and np.all(acc2[skipped] == 0) and np.all(rej2[skipped] == 0)
+    assert np.all(acc2[~skipped] + rej2[~skipped] > 0)
+
+
 @pytest.mark.parametrize("mode", ["plain", "persistent"])
 def test_attempt_cap_reports_convergence_failure(built_libs, mode):
     torch = _torch()
