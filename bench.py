@@ -97,6 +97,9 @@ def parse():
                     help="1: gradient of the whole window (every host step, two-level checkpoints, "
                          "WindowGradient); 0: of one 3600 s integrate().  Default: the window for ts1")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-check-cells", type=int, default=256,
+                    help="cells of the adjoint's accuracy check against central differences through the "
+                         "recorded steps (0: skip)")
     ap.add_argument("--tangent", type=int, default=0,
                     help="also time the tangent sweep over the adjoint section's checkpoints (mkpp_gpu_tangent)")
     ap.add_argument("--tail-after", type=int, default=None,
@@ -250,6 +253,73 @@ def bulk_rate(mechanism: str, cells: int, attempts: int, stream=None, defer: int
     flops = flops_per_attempt(load(mechanism))["total"]
     return {"cells": cells, "attempt_cap": attempts, "defer_after": defer, "attempts": att, "ms": ms,
             "attempts_per_s": att / (ms * 1e-3), "tflops": att * flops / (ms * 1e-3) / 1e12}
+
+
+def adjoint_accuracy_section(mechanism, raw, var_rows, solver, conc0, temp, rho, rh, param, seed, cells,
+                             max_attempts, checkpoints_cls, eps=1e-6) -> dict:
+    """Accuracy of the discrete adjoint on the bench's own cells, at the
+    adjoint section's setting (one 3600 s integrate(), loss sum (O3 - O3t)^2):
+    for one random direction in the variable species' initial concentrations
+    and one in the rate constants, each component eps x its value with a
+    random sign, the adjoint's directional derivative against a central
+    difference through the same recorded accepted steps (the replay).  Only
+    the GPU path runs here.  The relative error per cell is |fd - ad| /
+    max(|fd|, |ad|), over the cells that end with status 0 and finite values."""
+    import torch
+
+    f64 = torch.float64
+    dev = conc0.device
+    m = min(cells, conc0.shape[1])
+    c0 = conc0[:, :m].contiguous()
+    k, st_in = solver.rate_constants(c0, temp[:m].contiguous(), rho[:m].contiguous(), rh[:m].contiguous(),
+                                     None, param[:, :m].contiguous())
+    ck = checkpoints_cls(mechanism, m, 1536, dev)
+    c = c0.clone()
+    ck.forward(c, k, 3600.0, seed, max_attempts)
+    o3 = raw["species"].index("O3")
+    gen = torch.Generator(device="cpu").manual_seed(2718)
+    target = c[o3] * torch.exp(0.2 * torch.randn(m, generator=gen, dtype=f64)).to(dev)
+    lam = torch.zeros_like(c)
+    lam[o3] = 2.0 * (c[o3] - target)
+    gc, gk = ck.adjoint(k, lam)
+
+    def loss(x):
+        return (x[o3] - target) ** 2
+
+    def signs(shape):
+        return (torch.randint(0, 2, shape, generator=gen) * 2 - 1).to(device=dev, dtype=f64)
+
+    mask = torch.zeros((c0.shape[0], 1), dtype=f64, device=dev)
+    mask[list(var_rows)] = 1.0
+    dc = eps * c0.abs() * signs(c0.shape) * mask
+    cp, cm = c0 + dc, c0 - dc
+    ck.replay(cp, k)
+    ck.replay(cm, k)
+    fd_c, ad_c = (loss(cp) - loss(cm)) / 2, (gc * dc).sum(0)
+    dk = eps * k.abs() * signs(k.shape)
+    kp, km = k + dk, k - dk
+    cp, cm = c0.clone(), c0.clone()
+    ck.replay(cp, kp)
+    ck.replay(cm, km)
+    fd_k, ad_k = (loss(cp) - loss(cm)) / 2, (gk * dk).sum(0)
+    if dev.type == "cuda":
+        torch.cuda.synchronize()
+    ok = ((ck.status == 0) & (st_in == 0)).cpu().numpy()
+
+    def stats(fd, ad):
+        fd, ad = fd.cpu().numpy(), ad.cpu().numpy()
+        use = ok & np.isfinite(fd) & np.isfinite(ad)
+        rel = np.abs(fd - ad)[use] / np.maximum(np.maximum(np.abs(fd), np.abs(ad))[use], 1e-300)
+        if rel.size == 0:
+            return {"cells": 0}
+        return {"cells": int(rel.size), "median_rel_error": float(np.median(rel)),
+                "p90_rel_error": float(np.percentile(rel, 90)), "max_rel_error": float(rel.max()),
+                "frac_within_1e-4": float((rel <= 1e-4).mean())}
+
+    return {"config": f"first {m} cells, one 3600 s integrate(), the adjoint section's loss; central differences "
+                      f"(relative step {eps:g}, random signs) through the recorded accepted steps",
+            "initial_concentrations": stats(fd_c, ad_c), "rate_constants": stats(fd_k, ad_k),
+            "cells_status_ok": int(ok.sum())}
 
 
 def adjoint_window_section(w, hs, conc0, ktab, seed, args, stream, window_ms) -> dict:
@@ -902,6 +972,15 @@ def main():
             b["frac_of_fp64_peak"] = b["tflops"] / best if best else None
             result["bulk"] = b
             log(f"bulk: {b['tflops']:.3f} TFLOP/s with every lane busy")
+
+    if rank == 0 and world == 1 and not args.no_adjoint and not window_adjoint and args.adjoint_check_cells > 0:
+        with optional_section(result, "adjoint_accuracy", True):
+            from mkpp_gb300.adjoint import Checkpoints
+
+            result["adjoint_accuracy"] = adjoint_accuracy_section(
+                w.mechanism, raw, plan.var_phys, solver, conc0, temp, rho, rh, params[0], seed,
+                args.adjoint_check_cells, args.max_attempts, Checkpoints)
+            log(f"adjoint accuracy: {result['adjoint_accuracy']}")
 
     if rank == 0:
         print(json.dumps(result), flush=True)
