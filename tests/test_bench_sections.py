@@ -72,7 +72,8 @@ def test_adjoint_accuracy_section_matches_an_exact_adjoint():
         st = out[part]
         assert st["cells"] == 32
         assert st["max_rel_error"] < 1e-6, (part, st)
-        assert st["frac_within_1e-4"] == 1.0
+        assert st["frac_within_1e-4"] == 1.0 and st["frac_consistent"] == 1.0
+        assert st["median_difference_noise"] < 1e-6
 
 
 def test_adjoint_accuracy_section_sees_a_wrong_gradient():
@@ -91,6 +92,7 @@ def test_adjoint_accuracy_section_sees_a_wrong_gradient():
                                          conc0, 290.0 * one, one, one, torch.zeros((1, n), dtype=torch.float64),
                                          1e-6, n, 20000, Wrong)
     assert out["initial_concentrations"]["median_rel_error"] > 5e-3
+    assert out["initial_concentrations"]["frac_consistent"] == 0.0
     assert out["rate_constants"]["max_rel_error"] < 1e-6
 
 
