@@ -98,7 +98,9 @@ int mkpp_set_initial_step_seed(mkpp_handle_t handle, double seed);
  * reaches it reports MKPP_CELL_ERR_CONVERGENCE. */
 int mkpp_set_max_attempts(mkpp_handle_t handle, int max_attempts);
 /* Read back the per-cell status / accepted / rejected counts of the last
- * mkpp_integrate (each array num_cells ints; any may be NULL). */
+ * mkpp_integrate (each array num_cells ints; any may be NULL).  A cell
+ * skipped because its input is not finite (status 2) reports 0 accepted
+ * and 0 rejected steps for that call. */
 int mkpp_get_cell_stats(mkpp_handle_t handle, int* status, int* accepted, int* rejected);
 /* Cost ordering (default on): each mkpp_integrate hands out first the cells
  * that needed the most attempts in the previous call on this handle, so the
